@@ -1,0 +1,130 @@
+/*
+ * wsbb_gb300 — C-ABI of the GB300 (sm_103a) flowshop branch-and-bound hot
+ * path: batched begin-end child generation, LB2 Johnson two-machine bounds
+ * over all machine pairs, prune and compaction, and the exact DFS search
+ * built on them.
+ *
+ * Plain pointers and sizes only. Return codes: 0 = ok, negative = error
+ * (wsbb_last_error() describes the last failure on a context). The caller
+ * owns every buffer it passes; a context owns its device tables and its
+ * search pools. One context per host thread; calls on a context are
+ * stream-ordered on the stream they are given (NULL = the default stream)
+ * unless documented as synchronous.
+ *
+ * Reference interfaces each entry point replaces (vttuan/WSBB paths):
+ *   wsbb_ctx_create     bound_abstract::set_instance -> bound_flowshop::init
+ *                       (src/bound_flowshop.cpp:911-927, 953-956) and
+ *                       gpu::init / init_bound (src/gpu.cu:126-162,
+ *                       src/bound_flowshop_gpu.cu:398-433)
+ *   wsbb_lb2_eval       Evaluate_ON_GPU (src/bound_flowshop_gpu.cu:619-674)
+ *                       and bound_abstract::bornes_calculer
+ *                       (headers/bound_abstract.h:9-19,
+ *                       src/bound_flowshop.cpp:929-951)
+ *   wsbb_lb2_eval_host  gpu::decompose_on_cpu's H2D -> kernel -> D2H round
+ *                       trip (src/gpu.cu:211-234) for a caller-built pool
+ *   wsbb_explore        explorer::_explore_cpu / _explore_cpu_gpu
+ *                       (src/explorer.cu:92-148, 154-305) with
+ *                       decompose_beginend (src/decompose_beginend.cpp:26-107),
+ *                       gpu::prune (src/gpu.cu:257-408) and tree::take/insert
+ *                       (src/tree.cpp:257-304)
+ */
+#ifndef WSBB_GB300_H
+#define WSBB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WSBB_OK 0
+#define WSBB_ERR_ARG (-1)      /* bad argument or unsupported size */
+#define WSBB_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define WSBB_ERR_NOMEM (-3)    /* device or host allocation failed */
+#define WSBB_ERR_RANGE (-4)    /* processing times outside the table limits */
+#define WSBB_ERR_WATCHDOG (-5) /* a bounded device-side wait gave up */
+#define WSBB_ERR_CAPACITY (-6) /* search pool capacity exceeded */
+
+#define WSBB_MAX_JOBS 128     /* n <= 128 */
+#define WSBB_MAX_MACHINES 32  /* 2 <= m <= 32 */
+
+typedef struct wsbb_ctx wsbb_ctx;
+
+/*
+ * Node record (the pool format on the boundary; replaces the ~196-byte
+ * raw_bb_problem of the reference's missing bb_problem_calculator.h):
+ *
+ *   int16 job[n]    the permutation; job[0..limite1] is the front
+ *                   sequence, job[limite2..n-1] the back sequence
+ *   int16 limite1   last front position (-1: none)
+ *   int16 limite2   first back position (n: none); limite2 - limite1 == 1
+ *                   marks a leaf (complete permutation)
+ *   int16 depth     jobs fixed (informative; the bound does not read it)
+ *   int16 reserved
+ *   padding to wsbb_node_stride(n) bytes (a multiple of 16)
+ */
+size_t wsbb_node_stride(int n);
+
+/* Precompute the bound tables for an instance and upload them to `device`.
+ * p_mxn[k*n + j] = processing time of job j on machine k (the reference's
+ * machine-major stream order, src/instance_flowshop.cpp:88). Requires
+ * 2 <= n <= 128, 2 <= m <= 32, 0 <= p <= 65535 and every machine-pair lag
+ * (sum of p strictly between the two machines) <= 65535. */
+int wsbb_ctx_create(const int32_t *p_mxn, int n, int m, int device,
+                    wsbb_ctx **out);
+void wsbb_ctx_destroy(wsbb_ctx *ctx);
+const char *wsbb_last_error(const wsbb_ctx *ctx);
+
+/* Copies of the host-side precompute (for inspection and tests): pair
+ * machines (P each), lags and Johnson orders (P x n), static heads and
+ * tails (m). Any pointer may be NULL. */
+int wsbb_ctx_tables(const wsbb_ctx *ctx, int32_t *mach0, int32_t *mach1,
+                    int32_t *lag_pxn, int32_t *johnson_pxn, int32_t *heads,
+                    int32_t *tails);
+
+/* Host-only form of the same precompute (no device, no context): fills
+ * the same arrays wsbb_ctx_tables returns. */
+int wsbb_precompute(const int32_t *p_mxn, int n, int m, int32_t *mach0,
+                    int32_t *mach1, int32_t *lag_pxn, int32_t *johnson_pxn,
+                    int32_t *heads, int32_t *tails);
+
+/* Pool bounds on device memory, asynchronous on `stream`:
+ *   lb_out[i] = LB2 of record i (bornes_calculer with best = 999999), or
+ *   the makespan of its permutation when limite2 - limite1 == 1.
+ * `recs` holds `count` records of wsbb_node_stride(n) bytes, 16-byte
+ * aligned. */
+int wsbb_lb2_eval(wsbb_ctx *ctx, const void *recs, int64_t count,
+                  int32_t *lb_out, void *stream);
+/* One-machine bound LB1 = max_k(head_k + remaining work on k + tail_k),
+ * with LB2's head / tail conventions (leaf: makespan). */
+int wsbb_lb1_eval(wsbb_ctx *ctx, const void *recs, int64_t count,
+                  int32_t *lb_out, void *stream);
+/* Makespan of each record's full permutation (cursors ignored). */
+int wsbb_makespan_eval(wsbb_ctx *ctx, const void *recs, int64_t count,
+                       int32_t *out, void *stream);
+
+/* Synchronous host-buffer form of wsbb_lb2_eval: copies the records to the
+ * device, bounds them and copies the bounds back before returning. */
+int wsbb_lb2_eval_host(wsbb_ctx *ctx, const void *host_recs, int64_t count,
+                       int32_t *host_lb_out);
+
+/* Measured integer max-plus issue rate of `device` (add + max operations
+ * per second over every SM): the denominator of the LB2 kernel's
+ * roofline. Synchronous; allocates a few bytes of device memory. No
+ * counterpart in the reference. */
+int wsbb_probe_maxplus_peak(int device, double *ops_per_s);
+
+/* Host helpers (no device work). */
+void wsbb_gen_instance(uint64_t seed, int n, int m, int32_t *p_mxn);
+int32_t wsbb_neh(const int32_t *p_mxn, int n, int m, int32_t *perm_out);
+/* Seeded random pool in the record format (f in [0, n-3], b in
+ * [0, n-3-f]; a share of leaves). */
+int wsbb_gen_pool(uint64_t seed, int n, int64_t count, double leaf_share,
+                  void *recs_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

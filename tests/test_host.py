@@ -1,0 +1,99 @@
+"""Host-side product code (no GPU): the library loads and exports every
+declared symbol; its generator, pool maker, NEH and bound precompute equal
+the oracle's."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def W():
+    import wsbb_gb300
+    wsbb_gb300.lib()
+    return wsbb_gb300
+
+
+def declared_functions():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        txt = open(os.path.join(ROOT, "include", fn)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[\w]+\s*\*?\s*(wsbb_\w+)\s*\(", txt, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(W):
+    names = declared_functions()
+    assert len(names) >= 10
+    missing = [n for n in names if not hasattr(W.lib(), n)]
+    assert not missing, missing
+
+
+def test_instances_equal_oracle(W, oracle):
+    for (s, n, m) in [(0, 20, 20), (3, 50, 10), (7, 100, 20), (1, 5, 2)]:
+        np.testing.assert_array_equal(W.gen_instance(s, n, m), oracle.gen_instance(s, n, m))
+
+
+def test_pools_equal_oracle(W, oracle):
+    for (s, n, leaf) in [(1, 20, 0.05), (2, 50, 0.0), (9, 100, 0.2)]:
+        rec = W.gen_pool(s, n, 777, leaf)
+        perms, l1, l2 = W.unpack_records(rec, n)
+        o_perms, o_l1, o_l2 = oracle.random_pool(s, n, 777, leaf)
+        np.testing.assert_array_equal(perms, o_perms)
+        np.testing.assert_array_equal(l1, o_l1)
+        np.testing.assert_array_equal(l2, o_l2)
+
+
+def test_neh_equals_oracle(W, oracle):
+    for (s, n, m) in [(0, 20, 5), (1, 20, 20), (2, 50, 10), (4, 12, 3)]:
+        p = W.gen_instance(s, n, m)
+        c, perm = W.neh(p)
+        oc, operm = oracle.neh(p)
+        assert c == oc
+        np.testing.assert_array_equal(perm, operm)
+
+
+def test_precompute_equals_oracle(W, oracle, golden_pools):
+    keys = sorted({k.rsplit("_", 1)[0] for k in golden_pools.files})
+    for key in keys:
+        p = golden_pools[key + "_p"].astype(np.int32)
+        m, n = p.shape
+        P = m * (m - 1) // 2
+        got = {k: np.empty(s, dtype=np.int32) for k, s in
+               [("mach0", P), ("mach1", P), ("lag", P * n), ("johnson", P * n),
+                ("heads", m), ("tails", m)]}
+        rc = W.lib().wsbb_precompute(p.ctypes.data, n, m,
+                                     *(got[k].ctypes.data for k in
+                                       ("mach0", "mach1", "lag", "johnson", "heads", "tails")))
+        assert rc == 0
+        want = oracle.Bound(p).tables()
+        np.testing.assert_array_equal(got["mach0"], want["mach0"])
+        np.testing.assert_array_equal(got["mach1"], want["mach1"])
+        np.testing.assert_array_equal(got["lag"], want["lag"].ravel())
+        np.testing.assert_array_equal(got["johnson"], want["johnson"].ravel(), err_msg=key)
+        np.testing.assert_array_equal(got["heads"], want["min_arr"])
+        np.testing.assert_array_equal(got["tails"], want["min_dep"])
+
+
+def test_precompute_rejects_bad_sizes(W):
+    p = np.ones((40, 5), dtype=np.int32)
+    z = np.empty(4096, dtype=np.int32)
+    assert W.lib().wsbb_precompute(p.ctypes.data, 5, 40, *(z.ctypes.data,) * 6) != 0
+    p = np.ones((3, 200), dtype=np.int32)
+    assert W.lib().wsbb_precompute(p.ctypes.data, 200, 3, *(z.ctypes.data,) * 6) != 0
+
+
+def test_record_layout(W):
+    assert W.node_stride(20) == 48
+    assert W.node_stride(50) == 112
+    assert W.node_stride(100) == 208
+    rec = W.pack_records(np.arange(20)[None, :], [3], [17])
+    perms, l1, l2 = W.unpack_records(rec, 20)
+    assert (l1[0], l2[0]) == (3, 17)
+    assert rec.nbytes == 48

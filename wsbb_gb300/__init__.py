@@ -1,0 +1,9 @@
+"""wsbb_gb300 — GB300 (sm_103a) flowshop branch-and-bound hot path.
+
+Batched LB2 / LB1 / makespan bounds of begin-end nodes and the exact DFS
+search built on them, behind the C-ABI in include/wsbb_gb300.h. The Python
+modules are thin ctypes front ends over wsbb_gb300/_build/libwsbb_gb300.so.
+"""
+from ._lib import LIB_PATH, WsbbError, lib  # noqa: F401
+from .bound import (BoundFlowshopGB300, Context, gen_instance, gen_pool, neh,  # noqa: F401
+                    node_stride, pack_records, unpack_records)
