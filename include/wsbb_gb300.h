@@ -109,6 +109,50 @@ int wsbb_makespan_eval(wsbb_ctx *ctx, const void *recs, int64_t count,
 int wsbb_lb2_eval_host(wsbb_ctx *ctx, const void *host_recs, int64_t count,
                        int32_t *host_lb_out);
 
+/*
+ * Exact begin-end DFS search on the GPU.
+ *
+ * Same semantics as the reference CPU search (src/explorer.cu:92-148):
+ * the smallest rank path is taken first; leaves update the incumbent when
+ * strictly better; a node whose bound is not below the incumbent is pruned;
+ * otherwise its 2u children are bounded, the side is chosen with
+ * threshold `best` (decompose_beginend::choise) and the chosen side is
+ * ranked by (bound, job). Counters, optimum and optimal permutation equal
+ * the sequential search's exactly. The search state stays on the device;
+ * iterations are replayed from a CUDA graph.
+ */
+#define WSBB_EXPLORE_NO_GRAPH 1 /* launch iterations one by one */
+
+typedef struct {
+	int32_t ub0;         /* initial incumbent cost (INT32_MAX: none) */
+	int32_t best;        /* choise threshold (the reference default is 99999) */
+	int32_t window;      /* nodes branched per iteration (0: 4096) */
+	int32_t graph_iters; /* iterations per graph launch (0: 16) */
+	int64_t capacity;    /* stack capacity in nodes (0: 2^22) */
+	int64_t max_iters;   /* stop after this many iterations (0: none) */
+	int32_t flags;       /* WSBB_EXPLORE_* */
+	int32_t reserved;
+} wsbb_explore_cfg;
+
+typedef struct {
+	int64_t branched;   /* decomposed nodes (the reference's cpu_explored_nodes) */
+	int64_t pruned;     /* taken and pruned (boundedNodesDontExplore) */
+	int64_t leaves;     /* leaves taken */
+	int64_t improved;   /* incumbent improvements */
+	int64_t bounded;    /* child bounds of the search tree */
+	int64_t evaluated;  /* child bounds computed, including speculation */
+	int64_t discarded;  /* speculative entries dropped after improvements */
+	int64_t iterations;
+	int32_t best_cost;  /* final incumbent (INT32_MAX if none) */
+	int32_t status;     /* 0 complete, 1 iteration cap, <0 error */
+	uint64_t depth_hist[WSBB_MAX_JOBS + 1]; /* pruned + leaves per depth */
+	int32_t best_perm[WSBB_MAX_JOBS];       /* incumbent permutation */
+	double seconds;     /* device time of the search */
+} wsbb_stats;
+
+int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
+                 void *stream);
+
 /* Measured integer max-plus issue rate of `device` (add + max operations
  * per second over every SM): the denominator of the LB2 kernel's
  * roofline. Synchronous; allocates a few bytes of device memory. No

@@ -58,20 +58,25 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 		delete ctx;
 		return WSBB_ERR_ARG;
 	}
-	std::vector<uint8_t> blob = wsbb::pack_tables(ctx->inst, ctx->tables, err);
+	wsbb::HostTables H = wsbb::pack_tables(ctx->inst, err);
 	if (!err.empty()) {
 		fprintf(stderr, "wsbb_ctx_create: %s\n", err.c_str());
 		delete ctx;
 		return WSBB_ERR_RANGE;
 	}
 	ctx->device = device;
+	wsbb::DeviceTables &T = ctx->tables;
+	T.bytes = H.img8.size() + H.img16.size();
 	cudaError_t e = cudaSetDevice(device);
 	if (e == cudaSuccess)
 		e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
 	if (e == cudaSuccess)
-		e = cudaMalloc(&ctx->tables.blob, ctx->tables.bytes);
+		e = cudaMalloc(&T.mem, T.bytes);
+	uint8_t *base = static_cast<uint8_t *>(T.mem);
 	if (e == cudaSuccess)
-		e = cudaMemcpy(ctx->tables.blob, blob.data(), ctx->tables.bytes,
+		e = cudaMemcpy(base, H.img8.data(), H.img8.size(), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess && !H.img16.empty())
+		e = cudaMemcpy(base + H.img8.size(), H.img16.data(), H.img16.size(),
 		               cudaMemcpyHostToDevice);
 	if (e == cudaSuccess)
 		e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
@@ -80,17 +85,21 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 		wsbb_ctx_destroy(ctx);
 		return WSBB_ERR_CUDA;
 	}
+	T.t8 = H.t8;
+	T.t8.blob = base;
+	T.t16 = H.t16;
+	T.t16.blob = H.img16.empty() ? nullptr : base + H.img8.size();
 	wsbb::BoundParams &bp = ctx->bp;
-	bp.tables = static_cast<const uint8_t *>(ctx->tables.blob);
-	bp.table_bytes = uint32_t(ctx->tables.bytes);
-	bp.off_pt = ctx->tables.off_pt;
-	bp.off_pairs = ctx->tables.off_pairs;
-	bp.off_heads = ctx->tables.off_heads;
-	bp.off_tails = ctx->tables.off_tails;
+	bp.t8 = T.t8;
+	bp.t16 = T.t16;
 	bp.n = n;
 	bp.m = m;
 	bp.P = ctx->inst.P;
 	bp.stride = int(wsbb_node_stride(n));
+	int64_t total = 0;
+	for (int32_t v : ctx->inst.p)
+		total += v;
+	bp.col16 = total < 32768 ? 1 : 0;
 	*out = ctx;
 	return WSBB_OK;
 }
@@ -103,8 +112,8 @@ extern "C" void wsbb_ctx_destroy(wsbb_ctx *ctx)
 		return;
 	cudaSetDevice(ctx->device);
 	wsbb_explore_release(ctx);
-	if (ctx->tables.blob)
-		cudaFree(ctx->tables.blob);
+	if (ctx->tables.mem)
+		cudaFree(ctx->tables.mem);
 	if (ctx->d_recs)
 		cudaFree(ctx->d_recs);
 	if (ctx->d_out)

@@ -167,14 +167,15 @@ std::string build_instance(const int32_t *p, int n, int m, Instance &I)
 	return std::string();
 }
 
-std::vector<uint8_t> pack_tables(const Instance &I, DeviceTables &L,
-                                 std::string &err)
+namespace {
+
+// One table image: the Johnson table (entry_bytes per entry) then the
+// shared trailing arrays.
+std::vector<uint8_t> pack_image(const Instance &I, int entry_bytes, TableView &L)
 {
 	const int n = I.n, m = I.m, P = I.P;
 	auto align16 = [](size_t x) { return (x + 15) & ~size_t(15); };
-	size_t off = 0;
-	const size_t johnson_bytes = size_t(P) * n * 8;
-	off = align16(johnson_bytes);
+	size_t off = align16(size_t(P) * n * entry_bytes);
 	L.off_pt = uint32_t(off);
 	off = align16(off + size_t(m) * n * 4);
 	L.off_pairs = uint32_t(off);
@@ -183,10 +184,10 @@ std::vector<uint8_t> pack_tables(const Instance &I, DeviceTables &L,
 	off = align16(off + size_t(m) * 4);
 	L.off_tails = uint32_t(off);
 	off = align16(off + size_t(m) * 4);
-	L.bytes = off;
+	L.bytes = uint32_t(off);
 
-	std::vector<uint8_t> blob(L.bytes, 0);
-	uint32_t *jp = reinterpret_cast<uint32_t *>(blob.data());
+	std::vector<uint8_t> img(off, 0);
+	uint32_t *w = reinterpret_cast<uint32_t *>(img.data());
 	for (int i = 0; i < P; ++i) {
 		const int a = I.mach0[i], b = I.mach1[i];
 		for (int q = 0; q < n; ++q) {
@@ -194,19 +195,38 @@ std::vector<uint8_t> pack_tables(const Instance &I, DeviceTables &L,
 			const uint32_t p1 = uint32_t(I.p[a * n + j]);
 			const uint32_t p2 = uint32_t(I.p[b * n + j]);
 			const uint32_t lag = uint32_t(I.lag[size_t(i) * n + j]);
-			jp[2 * (size_t(i) * n + q)] = uint32_t(j) | (p1 << 16);
-			jp[2 * (size_t(i) * n + q) + 1] = p2 | (lag << 16);
+			const size_t e = size_t(i) * n + q;
+			if (entry_bytes == 8) {
+				w[2 * e] = uint32_t(j) | (p1 << 16);
+				w[2 * e + 1] = p2 | (lag << 16);
+			} else {
+				w[4 * e] = 1u << j;
+				w[4 * e + 1] = p1;
+				w[4 * e + 2] = p2;
+				w[4 * e + 3] = lag + p2;
+			}
 		}
 	}
-	std::memcpy(blob.data() + L.off_pt, I.p.data(), size_t(m) * n * 4);
-	int32_t *pairs = reinterpret_cast<int32_t *>(blob.data() + L.off_pairs);
+	std::memcpy(img.data() + L.off_pt, I.p.data(), size_t(m) * n * 4);
+	int32_t *pairs = reinterpret_cast<int32_t *>(img.data() + L.off_pairs);
 	for (int i = 0; i < P; ++i)
 		pairs[i] = I.mach0[i] | (I.mach1[i] << 8);
-	std::memcpy(blob.data() + L.off_heads, I.heads.data(), size_t(m) * 4);
-	std::memcpy(blob.data() + L.off_tails, I.tails.data(), size_t(m) * 4);
-	if (L.bytes > 200 * 1024)
+	std::memcpy(img.data() + L.off_heads, I.heads.data(), size_t(m) * 4);
+	std::memcpy(img.data() + L.off_tails, I.tails.data(), size_t(m) * 4);
+	return img;
+}
+
+}  // namespace
+
+HostTables pack_tables(const Instance &I, std::string &err)
+{
+	HostTables H;
+	H.img8 = pack_image(I, 8, H.t8);
+	if (I.n <= 32)
+		H.img16 = pack_image(I, 16, H.t16);
+	if (H.t8.bytes > 200 * 1024)
 		err = "bound tables exceed the shared-memory budget (n * m too large)";
-	return blob;
+	return H;
 }
 
 }  // namespace wsbb

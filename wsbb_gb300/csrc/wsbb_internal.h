@@ -29,32 +29,43 @@ struct Instance {
 // Fills `inst` from p (m x n). Returns an error message, empty on success.
 std::string build_instance(const int32_t *p_mxn, int n, int m, Instance &inst);
 
-// Device image of the bound tables. Each CTA stages it into shared memory
-// with one linear copy, so it is a single contiguous blob:
-//   uint2   johnson_packed[P * n]  pair-major, Johnson order:
-//                                  x = job | p[m1][job] << 16
-//                                  y = p[m2][job] | lag << 16
-//   int32   pt[m * n]              p, machine-major
-//   int32   pairs[P]               m1 | m2 << 8
-//   int32   heads[m], tails[m]
-struct DeviceTables {
-	void *blob = nullptr;
-	size_t bytes = 0;       // blob size, multiple of 16
-	uint32_t off_pt = 0;    // byte offsets inside the blob
-	uint32_t off_pairs = 0;
-	uint32_t off_heads = 0;
-	uint32_t off_tails = 0;
+// Device image of the bound tables. Each CTA stages one image into shared
+// memory with a single linear copy, so an image is one contiguous blob:
+//   johnson[P * n]   pair-major, each pair's jobs in Johnson order, as
+//     8-byte entries (generic path, any n <= 128):
+//       x = job | p[m1][job] << 16,  y = p[m2][job] | lag << 16
+//     16-byte entries (fast path, n <= 32):
+//       x = 1 << job, y = p[m1][job], z = p[m2][job], w = lag + p[m2][job]
+//   int32 pt[m * n]  p, machine-major
+//   int32 pairs[P]   m1 | m2 << 8
+//   int32 heads[m], tails[m]
+struct TableView {
+	const uint8_t *blob = nullptr;
+	uint32_t bytes = 0; // multiple of 16
+	uint32_t off_pt = 0, off_pairs = 0, off_heads = 0, off_tails = 0;
 };
 
-std::vector<uint8_t> pack_tables(const Instance &inst, DeviceTables &layout,
-                                 std::string &err);
+struct DeviceTables {
+	void *mem = nullptr; // both images in one allocation
+	size_t bytes = 0;
+	TableView t8, t16;   // t16.blob is null when n > 32
+};
+
+// Host images of the two tables; offsets are relative to each image.
+struct HostTables {
+	std::vector<uint8_t> img8, img16;
+	TableView t8, t16;
+};
+HostTables pack_tables(const Instance &inst, std::string &err);
 
 struct BoundParams {
-	const uint8_t *tables; // device blob
-	uint32_t table_bytes;
-	uint32_t off_pt, off_pairs, off_heads, off_tails;
+	TableView t8, t16;
 	int n, m, P;
 	int stride; // record stride in bytes
+	int col16;  // 1: every front/back time fits int16 (total work < 32768)
+	// When set, the kernels read the record count from device memory and
+	// the host-side count only sizes the grid (graph-captured launches).
+	const long long *count_dev = nullptr;
 };
 
 // Kernel launchers (bound_kernels.cu). `mode`: 0 = LB2, 1 = LB1,

@@ -1,0 +1,62 @@
+"""Python front end of the GPU search (wsbb_explore).
+
+`explore()` mirrors the reference CPU search (src/explorer.cu:92-148) with
+the same node semantics; the returned dict uses the reference's counter
+names where one exists (branched = cpu_explored_nodes, pruned =
+boundedNodesDontExplore).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from ._lib import WsbbError, lib
+from .bound import Context
+
+INT32_MAX = 2**31 - 1
+MAX_JOBS = 128
+
+
+class ExploreCfg(C.Structure):
+    _fields_ = [("ub0", C.c_int32), ("best", C.c_int32), ("window", C.c_int32),
+                ("graph_iters", C.c_int32), ("capacity", C.c_int64), ("max_iters", C.c_int64),
+                ("flags", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ExploreStats(C.Structure):
+    _fields_ = [("branched", C.c_int64), ("pruned", C.c_int64), ("leaves", C.c_int64),
+                ("improved", C.c_int64), ("bounded", C.c_int64), ("evaluated", C.c_int64),
+                ("discarded", C.c_int64), ("iterations", C.c_int64), ("best_cost", C.c_int32),
+                ("status", C.c_int32), ("depth_hist", C.c_uint64 * (MAX_JOBS + 1)),
+                ("best_perm", C.c_int32 * MAX_JOBS), ("seconds", C.c_double)]
+
+
+NO_GRAPH = 1
+
+
+def coverage(hist, n: int) -> int:
+    """Sum over pruned nodes and leaves of (n - depth)! (weights.cpp)."""
+    return sum(int(hist[d]) * math.factorial(n - d) for d in range(n + 1))
+
+
+def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int = 0,
+            graph_iters: int = 0, capacity: int = 0, max_iters: int = 0, graph: bool = True,
+            stream: int = 0) -> dict:
+    L = lib()
+    L.wsbb_explore.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    cfg = ExploreCfg(INT32_MAX if ub0 is None else int(ub0), int(best), int(window),
+                     int(graph_iters), int(capacity), int(max_iters), 0 if graph else NO_GRAPH, 0)
+    st = ExploreStats()
+    rc = L.wsbb_explore(ctx.h, C.byref(cfg), C.byref(st), stream or None)
+    if rc != 0:
+        raise WsbbError(rc, L.wsbb_last_error(ctx.h).decode())
+    n = ctx.n
+    return {"branched": st.branched, "pruned": st.pruned, "leaves": st.leaves,
+            "improved": st.improved, "bounded": st.bounded, "evaluated": st.evaluated,
+            "discarded": st.discarded, "iterations": st.iterations,
+            "best_cost": st.best_cost, "status": st.status,
+            "coverage": coverage(st.depth_hist, n),
+            "best_perm": np.array(st.best_perm[:n], dtype=np.int32),
+            "seconds": st.seconds}
