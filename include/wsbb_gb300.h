@@ -153,6 +153,36 @@ typedef struct {
 int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
                  void *stream);
 
+/*
+ * The same search for callers that cannot allocate GPU memory — code that
+ * runs under a memory budget fixed at start-up, inside a host callback or
+ * allocator hook where cudaMalloc may not be called, or on a path where an
+ * allocation failure mid-run is not acceptable. No counterpart in the
+ * reference.
+ *
+ * It makes no allocation of its own (no cudaMalloc / cudaFree, no events,
+ * no graph): the whole search state lives in one fixed device array of
+ * WSBB_NOALLOC_SCRATCH_BYTES that the library defines at file scope, and
+ * which every GPU that loads the library holds until the process exits.
+ * The context must exist already (wsbb_ctx_create allocates the instance
+ * tables). Limits: the stack capacity and window are derived from the
+ * fixed size — cfg->window 0 means 1024, cfg->capacity 0 means as many
+ * nodes as fit; a configuration that does not fit is rejected with
+ * WSBB_ERR_CAPACITY before anything runs, and a search that outgrows the
+ * capacity stops with WSBB_ERR_CAPACITY. Iterations are launched one by one
+ * (cfg->flags and cfg->graph_iters only set how often the host polls).
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. All calls share the one array and the search
+ * re-initialises what it reads, so consecutive calls are independent, but
+ * calls that overlap on the GPU (from two threads or two streams) race on
+ * the array and must be serialised by the caller.
+ */
+#define WSBB_NOALLOC_SCRATCH_BYTES (24u << 20)
+int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
+                         wsbb_stats *stats, void *stream);
+
 /* Measured integer max-plus issue rate of `device` (add + max operations
  * per second over every SM): the denominator of the LB2 kernel's
  * roofline. Synchronous; allocates a few bytes of device memory. No

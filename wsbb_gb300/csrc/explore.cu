@@ -45,6 +45,8 @@
 #include <chrono>
 #include <climits>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "wsbb_internal.h"
 
@@ -741,5 +743,177 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 	st->seconds = ms * 1e-3;
 	if (h.error)
 		return wsbb_set_error(ctx, h.error, "search pool capacity exceeded");
+	return WSBB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// wsbb_explore_noalloc: the search above with its whole state in one fixed
+// file-scope device array instead of memory it allocates, for callers that
+// must not allocate GPU memory. The kernels are the same; only where their
+// buffers live differs.
+
+namespace {
+
+__device__ __align__(256) uint8_t g_noalloc_scratch[WSBB_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device. In host
+// code the symbol itself is only a host-side stand-in, never a device
+// address, so it is never handed to a kernel directly.
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[64];
+
+int noalloc_scratch(wsbb_ctx *ctx, uint8_t **out)
+{
+	if (ctx->device < 0 || ctx->device >= 64)
+		return wsbb_set_error(ctx, WSBB_ERR_ARG, "device ordinal out of range");
+	std::lock_guard<std::mutex> lock(g_noalloc_mu);
+	if (!g_noalloc_addr[ctx->device]) {
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if (e != cudaSuccess || !p)
+			return ex_fail(ctx, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+			               "cudaGetSymbolAddress(no-alloc scratch)");
+		g_noalloc_addr[ctx->device] = p;
+	}
+	*out = static_cast<uint8_t *>(g_noalloc_addr[ctx->device]);
+	return WSBB_OK;
+}
+
+// Lays the search buffers out from `base` (null: only sizes them).
+size_t noalloc_layout(uint8_t *base, long long cap, int window, int n, int S,
+                      wsbb::ExParams &P)
+{
+	using wsbb::ExDev;
+	using wsbb::Meta;
+	const long long region_cap = 4ll * window + 4096;
+	const long long child_cap = (long long)window * 2 * n;
+	auto a256 = [](size_t v) { return (v + 255) & ~size_t(255); };
+	size_t off = 0;
+	auto take = [&](size_t bytes) {
+		const size_t at = off;
+		off = a256(off + bytes);
+		return base ? base + at : nullptr;
+	};
+	P.dev = reinterpret_cast<ExDev *>(take(sizeof(ExDev)));
+	P.rec = take(size_t(cap) * S);
+	P.meta = reinterpret_cast<Meta *>(take(size_t(cap) * sizeof(Meta)));
+	P.tmp_rec = take(size_t(region_cap) * S);
+	P.tmp_meta = reinterpret_cast<Meta *>(take(size_t(region_cap) * sizeof(Meta)));
+	P.slot_from_top = reinterpret_cast<long long *>(take(size_t(region_cap) * 8));
+	P.father_of = reinterpret_cast<int *>(take(size_t(region_cap) * 4));
+	P.father_ridx = reinterpret_cast<long long *>(take(size_t(window) * 8));
+	P.child_off = reinterpret_cast<long long *>(take(size_t(window + 1) * 8));
+	P.child_rec = take(size_t(child_cap) * S);
+	P.child_lb = reinterpret_cast<int32_t *>(take(size_t(child_cap) * 4));
+	P.child_job = reinterpret_cast<int16_t *>(take(size_t(child_cap) * 2));
+	P.best_rec = take(size_t(S));
+	P.cap = cap;
+	P.region_cap = region_cap;
+	P.child_cap = child_cap;
+	P.window = window;
+	P.n = n;
+	P.stride = S;
+	return off;
+}
+
+}  // namespace
+
+extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
+                                    wsbb_stats *st, void *stream_v)
+{
+	using namespace wsbb;
+	if (!ctx || !cfg || !st)
+		return WSBB_ERR_ARG;
+	cudaError_t e = cudaSetDevice(ctx->device);
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "cudaSetDevice");
+	uint8_t *scratch = nullptr;
+	int rc = noalloc_scratch(ctx, &scratch);
+	if (rc != WSBB_OK)
+		return rc;
+
+	const int n = ctx->inst.n;
+	const int S = ctx->bp.stride;
+	const int window = cfg->window > 0 ? cfg->window : 1024;
+	const size_t limit = WSBB_NOALLOC_SCRATCH_BYTES;
+	ExploreState X; // host-side view only: no graph, no allocation
+	if (window > (1 << 20))
+		return wsbb_set_error(ctx, WSBB_ERR_ARG, "window out of range");
+	long long cap = cfg->capacity;
+	if (cap <= 0) {
+		const size_t fixed = noalloc_layout(nullptr, 0, window, n, S, X.P);
+		cap = fixed < limit ? (long long)((limit - fixed) / (S + sizeof(Meta))) : 0;
+		while (cap > 0 && noalloc_layout(nullptr, cap, window, n, S, X.P) > limit)
+			cap -= 256;
+	}
+	const long long region_cap = 4ll * window + 4096;
+	if (cap < region_cap || noalloc_layout(nullptr, cap, window, n, S, X.P) > limit)
+		return wsbb_set_error(ctx, WSBB_ERR_CAPACITY,
+		                      "window / capacity do not fit the fixed no-alloc scratch of " +
+		                          std::to_string(limit >> 20) + " MiB");
+	noalloc_layout(scratch, cap, window, n, S, X.P);
+	X.cap = cap;
+	X.region_cap = region_cap;
+	X.child_cap = X.P.child_cap;
+	X.window = window;
+	X.child_bp = ctx->bp;
+	X.child_bp.count_dev = &X.P.dev->n_children;
+
+	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
+	const auto t0 = std::chrono::steady_clock::now();
+	init_kernel<<<1, 128, 0, s>>>(X.P, cfg->ub0, cfg->best);
+	e = cudaGetLastError();
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "search init");
+	const int G = cfg->graph_iters > 0 ? cfg->graph_iters : 16;
+	const long long max_iters = cfg->max_iters > 0 ? cfg->max_iters : LLONG_MAX;
+	ExDev h{};
+	long long launched = 0;
+	int status = 0;
+	for (;;) {
+		for (int i = 0; i < G && e == cudaSuccess; ++i)
+			e = enqueue_iteration(ctx, X, s);
+		launched += G;
+		if (e != cudaSuccess)
+			break;
+		e = cudaMemcpyAsync(&h, X.P.dev, sizeof(ExDev), cudaMemcpyDeviceToHost, s);
+		if (e == cudaSuccess)
+			e = cudaStreamSynchronize(s);
+		if (e != cudaSuccess || h.done || h.error)
+			break;
+		if (launched >= max_iters) {
+			status = 1;
+			break;
+		}
+	}
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "no-alloc search");
+	int16_t best_rec[WSBB_MAX_JOBS + 8];
+	e = cudaMemcpyAsync(best_rec, X.P.best_rec, S, cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(s);
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "incumbent download");
+	const double secs =
+	    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+
+	std::memset(st, 0, sizeof(*st));
+	st->branched = (int64_t)h.branched;
+	st->pruned = (int64_t)h.pruned;
+	st->leaves = (int64_t)h.leaves;
+	st->improved = (int64_t)h.improved;
+	st->bounded = (int64_t)h.bounded;
+	st->evaluated = (int64_t)h.evaluated;
+	st->discarded = (int64_t)h.discarded;
+	st->iterations = (int64_t)h.iterations;
+	st->best_cost = h.ub;
+	st->status = h.error ? h.error : status;
+	for (int d = 0; d <= n; ++d)
+		st->depth_hist[d] = h.hist[d];
+	for (int j = 0; j < n; ++j)
+		st->best_perm[j] = best_rec[j];
+	st->seconds = secs;
+	if (h.error)
+		return wsbb_set_error(ctx, h.error, "search outgrew the no-alloc scratch capacity");
 	return WSBB_OK;
 }
