@@ -148,6 +148,8 @@ typedef struct {
 	uint64_t depth_hist[WSBB_MAX_JOBS + 1]; /* pruned + leaves per depth */
 	int32_t best_perm[WSBB_MAX_JOBS];       /* incumbent permutation */
 	double seconds;     /* device time of the search */
+	int64_t scanned;    /* stack entries scanned to select fathers */
+	int64_t committed;  /* stack entries committed */
 } wsbb_stats;
 
 int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,

@@ -85,7 +85,7 @@ def test_capacity_error_is_reported(W):
     p = Wm.gen_instance(2, 20, 5)
     ctx = Wm.Context(p)
     with pytest.raises(Wm.WsbbError) as ei:
-        E.explore(ctx, window=4096, capacity=4 * 4096 + 4096)
+        E.explore(ctx, window=4096, capacity=16 * 4096 + 8192)
     assert ei.value.code == -6
     # the context stays usable
     got = E.explore(ctx, window=64)

@@ -12,35 +12,51 @@
 //
 // Here the whole DFS stack lives in HBM, sorted by rank path (index 0 is
 // the bottom, the top entry is the next node the sequential search takes).
-// Every iteration is four stream-ordered kernels:
+// Every iteration is a fixed sequence of stream-ordered kernels (replayed
+// from a CUDA graph):
 //
-//   commit_select (1 CTA)  Commit, in DFS order, everything already decided
-//                          at the top of the stack: leaves (incumbent
-//                          updates), pruned markers, and markers of nodes
-//                          that were branched ahead of their turn — each
-//                          re-checked against the incumbent the sequential
-//                          search would have at that point; a marker that
-//                          fails is counted as pruned and its speculative
-//                          subtree (contiguous just below it) is dropped.
-//                          Then select the next `window` unprocessed nodes
-//                          below the top: bound >= incumbent marks them
-//                          pruned (final: the incumbent only decreases),
-//                          the others become this iteration's fathers.
-//   make_children          Copy the rewrite region aside and write every
-//                          father's 2u children (both sides) or 2 leaves
-//                          as pool records (create_raw_problem3,
-//                          src/bb_problem_calculator.cpp:25-79).
-//   lb2_pool_kernel        Bound the children (bound_kernels.cu).
-//   emit                   Per father: side choice, ranks, and the
-//                          rewritten region — chosen children (worst rank
-//                          lowest) under a BRANCHED marker that keeps the
-//                          father's bound for its commit-time check.
+//   commit (1 CTA)      Commit, in DFS order, everything already decided at
+//                       the top of the stack: leaves (incumbent updates),
+//                       pruned entries, and markers of nodes that were
+//                       branched ahead of their turn — each re-checked
+//                       against the incumbent the sequential search holds at
+//                       that point; a marker that fails is counted as pruned
+//                       and its speculative subtree (contiguous just below
+//                       it) is dropped.
+//   doom (1 warp)       Only after the incumbent improved: walk the top of
+//                       the stack and settle markers that the new incumbent
+//                       already condemns — the sequential search will prune
+//                       them whenever it reaches them, since the incumbent
+//                       never increases — so their subtrees are marked dead
+//                       and never expanded further.
+//   select (3 kernels)  Count the unprocessed nodes of the top region per
+//                       chunk (bound >= incumbent prunes them, final), plan
+//                       the first `window` of them, and mark those fathers.
+//   father scan         Child offsets of the fathers.
+//   make_children       Copy the rewrite region aside and write every
+//                       father's 2u children (both sides) or 2 leaves as pool
+//                       records (create_raw_problem3,
+//                       src/bb_problem_calculator.cpp:25-79).
+//   lb2 pool kernel     Bound the children (bound_kernels.cu).
+//   choose              Per father: side choice with threshold `best`, ranks
+//                       of the kept side by (bound, job), and how many of
+//                       them the incumbent already prunes.
+//   kept scan           Block sizes of the fathers in the rewritten region.
+//   emit                Scatter: the chosen children still open (their lowest
+//                       ranks) under a BRANCHED marker that keeps the
+//                       father's bound for its commit-time check and the
+//                       count of its children pruned at birth (the highest
+//                       ranks, which never need an entry); other region
+//                       entries move to their new slots.
 //
-// Node counts, the incumbent trace and the optimum therefore equal the
-// sequential search's exactly; work spent on markers that later fail is
-// reported separately (evaluated vs bounded, discarded). No kernel waits
-// on another CTA, so nothing can spin; an iteration cap and a capacity
-// check end the search with a status instead.
+// Counts are only taken at commit, in the sequential order, so node counts,
+// the incumbent trace and the optimum equal the sequential search's
+// exactly; work on markers that later fail is reported separately
+// (evaluated vs bounded, discarded). The number of fathers per iteration
+// adapts: it drops to its minimum when the incumbent improves (speculation
+// made then is the kind that gets discarded) and doubles while it does not.
+// No kernel waits on another CTA, so nothing can spin; an iteration cap and
+// a capacity check end the search with a status instead.
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -53,13 +69,22 @@
 namespace wsbb {
 namespace {
 
-enum : uint8_t { ST_UNPROC = 0, ST_LEAF = 1, ST_PRUNED = 2, ST_BRANCHED = 3 };
+// CONDEMNED: a marker the incumbent already prunes whose whole subtree is
+// marked DEAD, so commit can count it as pruned without walking the subtree.
+enum : uint8_t {
+	ST_UNPROC = 0,
+	ST_LEAF = 1,
+	ST_PRUNED = 2,
+	ST_BRANCHED = 3,
+	ST_DEAD = 4,
+	ST_CONDEMNED = 5
+};
 
 struct Meta {
 	int32_t lb;
-	int16_t depth;
+	uint8_t depth;
 	uint8_t state;
-	uint8_t pad;
+	uint16_t npruned; // BRANCHED: chosen children already pruned when emitted
 };
 static_assert(sizeof(Meta) == 8, "Meta is 8 bytes");
 
@@ -72,31 +97,47 @@ struct ExDev {
 	long long n_children;   // child records to bound this iteration
 	long long iterations;
 	int ub, best, done, error;
+	int win, win_min, win_max, doom;
 	unsigned long long branched, pruned, leaves, improved, bounded;
-	unsigned long long evaluated, discarded;
+	unsigned long long evaluated, discarded, scanned, committed;
 	unsigned long long hist[WSBB_MAX_JOBS + 1];
 };
 
 struct ExParams {
 	ExDev *dev;
-	uint8_t *rec;           // stack records [cap][stride]
-	Meta *meta;             // stack meta [cap]
-	uint8_t *tmp_rec;       // region copy [region_cap][stride]
-	Meta *tmp_meta;         // [region_cap]
-	long long *slot_from_top; // [region_cap] slots above the entry after rewrite
-	int *father_of;         // [region_cap] father ordinal or -1
-	long long *father_ridx; // [window] region index of each father
-	long long *child_off;   // [window + 1] first child record of each father
-	uint8_t *child_rec;     // [child_cap][stride]
-	int32_t *child_lb;      // [child_cap]
-	int16_t *child_job;     // [child_cap] job moved by the branching
-	uint8_t *best_rec;      // [stride] incumbent permutation record
+	uint8_t *rec;             // stack records [cap][stride]
+	Meta *meta;               // stack meta [cap]
+	uint8_t *tmp_rec;         // region copy [region_cap][stride]
+	Meta *tmp_meta;           // [region_cap]
+	int *fathers_before;      // [region_cap] fathers above each region entry
+	int *father_of;           // [region_cap] father ordinal or -1
+	int *chunk_cnt;           // [n_chunks] candidates per select chunk
+	long long *father_ridx;   // [window] region index of each father
+	long long *child_off;     // [window + 1] first child record of each father
+	int *father_children;     // [window] child records of each father
+	int *father_side;         // [window] offset of the chosen side in its children
+	int *father_kept;         // [window] chosen children still open
+	int *father_npr;          // [window] chosen children pruned at birth
+	long long *kept_before;   // [window + 1] slots of the father blocks above
+	uint8_t *child_rec;       // [child_cap][stride]
+	int32_t *child_lb;        // [child_cap]
+	int16_t *child_job;       // [child_cap] job moved by the branching
+	int32_t *child_rank;      // [child_cap] rank within the chosen side
+	uint8_t *best_rec;        // [stride] incumbent permutation record
 	long long cap, region_cap, child_cap;
-	int window;
+	int window;               // maximum fathers per iteration
+	int n_chunks;             // select chunks covering region_cap
 	int n, stride;
 };
 
 constexpr int kSelThreads = 1024;
+// Entries per thread in the single-CTA scans: one block-scan round covers
+// kItems * kSelThreads stack entries.
+constexpr int kItems = 8;
+constexpr int kChunk = kItems * kSelThreads;
+// Select chunks: one 256-thread CTA scans kSelChunk entries.
+constexpr int kSelCtaThreads = 256;
+constexpr int kSelChunk = kItems * kSelCtaThreads;
 
 __device__ __forceinline__ int children_of_depth(int depth, int n)
 {
@@ -104,13 +145,9 @@ __device__ __forceinline__ int children_of_depth(int depth, int n)
 	return depth == n - 2 ? 2 : 2 * (n - depth);
 }
 
-__device__ __forceinline__ int kept_of_depth(int depth, int n)
-{
-	return depth == n - 2 ? 2 : (n - depth);
-}
-
-// Block-wide scans for kSelThreads threads. `scratch` holds 32 values.
-template <typename T, typename Op>
+// Block-wide exclusive scan for NT threads; `scratch` holds 32 values;
+// `total` (optional) receives the block total.
+template <int NT, typename T, typename Op>
 __device__ T block_excl_scan(T v, Op op, T identity, T *scratch, T *total)
 {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -125,7 +162,7 @@ __device__ T block_excl_scan(T v, Op op, T identity, T *scratch, T *total)
 		scratch[warp] = x;
 	__syncthreads();
 	if (warp == 0) {
-		T w = lane < (kSelThreads / 32) ? scratch[lane] : identity;
+		T w = lane < (NT / 32) ? scratch[lane] : identity;
 #pragma unroll
 		for (int d = 1; d < 32; d <<= 1) {
 			T y = __shfl_up_sync(0xffffffffu, w, d);
@@ -135,93 +172,149 @@ __device__ T block_excl_scan(T v, Op op, T identity, T *scratch, T *total)
 		scratch[lane] = w; // inclusive over warps
 	}
 	__syncthreads();
-	T warp_prefix = warp == 0 ? identity : scratch[warp - 1];
-	T incl = op(warp_prefix, x);
-	T excl_in_warp = __shfl_up_sync(0xffffffffu, x, 1);
-	T excl = lane == 0 ? warp_prefix : op(warp_prefix, excl_in_warp);
+	const T warp_prefix = warp == 0 ? identity : scratch[warp - 1];
+	const T excl_in_warp = __shfl_up_sync(0xffffffffu, x, 1);
+	const T excl = lane == 0 ? warp_prefix : op(warp_prefix, excl_in_warp);
 	if (total)
-		*total = scratch[kSelThreads / 32 - 1];
+		*total = scratch[NT / 32 - 1];
 	__syncthreads();
-	(void)incl;
 	return excl;
 }
 
-template <typename T, typename Op>
+template <int NT, typename T, typename Op>
 __device__ T block_reduce(T v, Op op, T identity, T *scratch)
 {
 	T total;
-	block_excl_scan(v, op, identity, scratch, &total);
+	block_excl_scan<NT>(v, op, identity, scratch, &total);
 	return total;
 }
 
 struct MinOp {
 	__device__ int operator()(int a, int b) const { return a < b ? a : b; }
 };
-struct SumOp {
-	__device__ long long operator()(long long a, long long b) const { return a + b; }
-};
 struct MaxOp {
 	__device__ int operator()(int a, int b) const { return a > b ? a : b; }
 };
+struct SumOp {
+	__device__ long long operator()(long long a, long long b) const { return a + b; }
+};
+struct IntSumOp {
+	__device__ int operator()(int a, int b) const { return a + b; }
+};
 
-__global__ void __launch_bounds__(kSelThreads) commit_select_kernel(ExParams P)
+__device__ __forceinline__ bool halted(const ExDev *D) { return D->done || D->error; }
+
+// ---- commit: walk down from the top in DFS order -------------------------
+__global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 {
 	__shared__ int s_int[32];
-	__shared__ long long s_ll[32];
-	__shared__ unsigned long long s_cnt[5];
+	__shared__ unsigned long long s_cnt[6];
 	__shared__ unsigned long long s_hist[WSBB_MAX_JOBS + 1];
 	ExDev *D = P.dev;
-	if (D->done || D->error)
+	if (halted(D))
 		return;
 	const int t = threadIdx.x;
 	const int n = P.n;
-	if (t < 5)
+	if (t < 6)
 		s_cnt[t] = 0;
 	for (int i = t; i <= n; i += kSelThreads)
 		s_hist[i] = 0;
 	__syncthreads();
 
 	long long top = D->top;
-	int ub = D->ub;
+	const int ub0 = D->ub;
+	int ub = ub0;
+	unsigned long long c_br = 0, c_pr = 0, c_lf = 0, c_im = 0, c_bd = 0, c_dead = 0;
 
-	// ---- commit -------------------------------------------------------
 	while (top >= 0) {
-		const long long idx = top - t;
-		Meta e = {INT_MAX, 0, ST_UNPROC, 0};
-		if (idx >= 0)
-			e = P.meta[idx];
-		const int leaf_cost = (idx >= 0 && e.state == ST_LEAF) ? e.lb : INT_MAX;
-		const int ub_before = min(ub, block_excl_scan(leaf_cost, MinOp(), INT_MAX, s_int,
-		                                              (int *)nullptr));
-		const bool stop = idx < 0 || e.state == ST_UNPROC ||
-		                  (e.state == ST_BRANCHED && e.lb >= ub_before);
-		const int s = block_reduce(stop ? t : kSelThreads, MinOp(), kSelThreads, s_int);
-		if (t < s) {
-			if (e.state == ST_BRANCHED) {
-				atomicAdd(&s_cnt[0], 1ull);
-				atomicAdd(&s_cnt[4], (unsigned long long)children_of_depth(e.depth, n));
-			} else if (e.state == ST_PRUNED) {
-				atomicAdd(&s_cnt[1], 1ull);
-				atomicAdd(&s_hist[e.depth], 1ull);
-			} else { // leaf
-				atomicAdd(&s_cnt[2], 1ull);
-				atomicAdd(&s_hist[n], 1ull);
-				if (e.lb < ub_before)
-					atomicAdd(&s_cnt[3], 1ull);
+		// thread t holds entries top - (kItems*t + i), i = 0 nearest the top
+		Meta e[kItems];
+		int leaf_min = INT_MAX;
+#pragma unroll
+		for (int i = 0; i < kItems; ++i) {
+			const long long idx = top - (long long)(kItems * t + i);
+			e[i] = idx >= 0 ? P.meta[idx] : Meta{INT_MAX, 0, ST_UNPROC, 0};
+			if (idx >= 0 && e[i].state == ST_LEAF)
+				leaf_min = min(leaf_min, e[i].lb);
+		}
+		const int ub_in = min(ub, block_excl_scan<kSelThreads>(leaf_min, MinOp(), INT_MAX, s_int,
+		                                                       (int *)nullptr));
+		// first entry that cannot be committed: an unprocessed node, the
+		// stack bottom, or a marker failing against the running incumbent
+		int first_stop = kChunk;
+		{
+			int u = ub_in;
+#pragma unroll
+			for (int i = 0; i < kItems; ++i) {
+				const long long idx = top - (long long)(kItems * t + i);
+				const bool stop = idx < 0 || e[i].state == ST_UNPROC ||
+				                  (e[i].state == ST_BRANCHED && e[i].lb >= u);
+				if (stop && first_stop == kChunk)
+					first_stop = kItems * t + i;
+				if (e[i].state == ST_LEAF)
+					u = min(u, e[i].lb);
 			}
 		}
-		const int chunk_min = block_reduce(t < s ? leaf_cost : INT_MAX, MinOp(), INT_MAX, s_int);
-		if (chunk_min < ub) {
+		const int s = block_reduce<kSelThreads>(first_stop, MinOp(), kChunk, s_int);
+		int chunk_min = INT_MAX, first_min = kChunk;
+		{
+			int u = ub_in;
+#pragma unroll
+			for (int i = 0; i < kItems; ++i) {
+				const int g = kItems * t + i;
+				// coverage histogram: (depth, count) of what this entry adds
+				int hkey = 255;
+				unsigned hval = 0;
+				if (g < s) {
+					if (e[i].state == ST_BRANCHED) {
+						c_br++;
+						c_bd += (unsigned long long)children_of_depth(e[i].depth, n);
+						if (e[i].npruned) {
+							c_pr += e[i].npruned;
+							hkey = e[i].depth + 1;
+							hval = e[i].npruned;
+						}
+					} else if (e[i].state == ST_PRUNED || e[i].state == ST_CONDEMNED) {
+						c_pr++;
+						hkey = e[i].depth;
+						hval = 1;
+					} else if (e[i].state == ST_DEAD) {
+						c_dead++; // inside a subtree the sequential search prunes
+					} else { // leaf
+						c_lf++;
+						hkey = n;
+						hval = 1;
+						if (e[i].lb < u)
+							c_im++;
+						u = min(u, e[i].lb);
+						if (e[i].lb < chunk_min) {
+							chunk_min = e[i].lb;
+							first_min = g;
+						}
+					}
+				}
+				// one shared atomic per distinct depth per warp: most entries
+				// of a chunk share a few depths
+				const unsigned grp = __match_any_sync(0xffffffffu, hkey);
+				const unsigned sum = __reduce_add_sync(grp, hval);
+				if (hkey != 255 && (threadIdx.x & 31) == __ffs(grp) - 1)
+					atomicAdd(&s_hist[hkey], (unsigned long long)sum);
+			}
+		}
+		const int cmin = block_reduce<kSelThreads>(chunk_min, MinOp(), INT_MAX, s_int);
+		if (cmin < ub) {
 			// the first leaf reaching the new minimum is the one that set it
-			const int first = block_reduce((t < s && leaf_cost == chunk_min) ? t : kSelThreads,
-			                               MinOp(), kSelThreads, s_int);
+			const int first = block_reduce<kSelThreads>(chunk_min == cmin ? first_min : kChunk,
+			                                            MinOp(), kChunk, s_int);
 			const long long src = top - first;
 			for (int b = t; b < P.stride; b += kSelThreads)
 				P.best_rec[b] = P.rec[src * P.stride + b];
-			ub = chunk_min;
+			ub = cmin;
 		}
 		top -= s;
-		if (s == kSelThreads)
+		if (t == 0)
+			D->committed += (unsigned long long)s;
+		if (s == kChunk)
 			continue;
 		if (top < 0)
 			break;
@@ -232,102 +325,237 @@ __global__ void __launch_bounds__(kSelThreads) commit_select_kernel(ExParams P)
 		// search would hold here: that node is pruned, and everything
 		// speculatively built under it is dropped.
 		if (t == 0) {
-			s_cnt[1] += 1;
-			s_hist[stopper.depth] += 1;
+			c_pr++;
+			atomicAdd(&s_hist[stopper.depth], 1ull);
 		}
-		__syncthreads();
 		top -= 1;
 		while (top >= 0) {
-			const long long j = top - t;
-			const bool out = j < 0 || P.meta[j].depth <= stopper.depth;
-			const int s2 = block_reduce(out ? t : kSelThreads, MinOp(), kSelThreads, s_int);
+			int out_at = kChunk;
+#pragma unroll
+			for (int i = 0; i < kItems; ++i) {
+				const long long j = top - (long long)(kItems * t + i);
+				const bool out = j < 0 || P.meta[j].depth <= stopper.depth;
+				if (out && out_at == kChunk)
+					out_at = kItems * t + i;
+			}
+			const int s2 = block_reduce<kSelThreads>(out_at, MinOp(), kChunk, s_int);
 			if (t == 0)
 				D->discarded += (unsigned long long)s2;
 			top -= s2;
-			if (s2 < kSelThreads)
+			if (s2 < kChunk)
 				break;
 		}
 	}
 
-	// ---- select -------------------------------------------------------
-	long long nf = 0, region = 0, slots = 0, nchild = 0;
-	const long long scan_limit = P.region_cap;
-	while (nf < P.window && top - region >= 0 && region < scan_limit) {
-		const long long ridx = region + t;
-		const long long idx = top - ridx;
-		const bool valid = idx >= 0 && ridx < scan_limit;
-		Meta e = {0, 0, ST_LEAF, 0};
-		if (valid)
-			e = P.meta[idx];
-		const bool unproc = valid && e.state == ST_UNPROC;
-		if (unproc && e.lb >= ub) {
-			P.meta[idx].state = ST_PRUNED; // final: the incumbent only decreases
-			e.state = ST_PRUNED;
-		}
-		const bool cand = unproc && e.lb < ub;
-		long long ncand_chunk;
-		const long long before = block_excl_scan<long long>(cand ? 1 : 0, SumOp(), 0ll, s_ll,
-		                                                    &ncand_chunk);
-		const bool take = cand && nf + before < P.window;
-		// the region ends at the last father taken, or at the chunk's end
-		int last;
-		if (nf + ncand_chunk >= P.window)
-			last = block_reduce((cand && nf + before == P.window - 1) ? t : -1, MaxOp(), -1,
-			                    s_int);
-		else
-			last = block_reduce(valid ? t : -1, MaxOp(), -1, s_int);
-		const bool in_region = t <= last;
-		const long long my_slots =
-		    in_region ? (take ? 1 + kept_of_depth(e.depth, n) : 1) : 0;
-		long long chunk_slots;
-		const long long slot_before =
-		    block_excl_scan<long long>(my_slots, SumOp(), 0ll, s_ll, &chunk_slots);
-		const long long my_children = take ? children_of_depth(e.depth, n) : 0;
-		long long chunk_children;
-		const long long child_before =
-		    block_excl_scan<long long>(my_children, SumOp(), 0ll, s_ll, &chunk_children);
-		if (in_region) {
-			P.slot_from_top[ridx] = slots + slot_before;
-			P.father_of[ridx] = take ? int(nf + before) : -1;
-			if (take) {
-				P.father_ridx[nf + before] = ridx;
-				P.child_off[nf + before] = nchild + child_before;
-			}
-		}
-		const long long taken = min(ncand_chunk, (long long)P.window - nf);
-		nf += taken;
-		slots += chunk_slots;
-		nchild += chunk_children;
-		region += last + 1;
-		if (last + 1 < kSelThreads && nf < P.window)
-			break; // reached the bottom of the stack
-	}
-
-	const long long new_top = top - region + slots;
+	atomicAdd(&s_cnt[0], c_br);
+	atomicAdd(&s_cnt[1], c_pr);
+	atomicAdd(&s_cnt[2], c_lf);
+	atomicAdd(&s_cnt[3], c_im);
+	atomicAdd(&s_cnt[4], c_bd);
+	atomicAdd(&s_cnt[5], c_dead);
+	__syncthreads();
 	if (t == 0) {
-		P.child_off[nf] = nchild;
-		if (nf > 0 && (new_top >= P.cap || nchild > P.child_cap)) {
-			D->error = WSBB_ERR_CAPACITY;
-		}
 		D->branched += s_cnt[0];
 		D->pruned += s_cnt[1];
 		D->leaves += s_cnt[2];
 		D->improved += s_cnt[3];
 		D->bounded += s_cnt[4];
+		D->discarded += s_cnt[5];
 		D->ub = ub;
 		D->top = top;
-		D->region_len = nf > 0 ? region : 0;
-		D->region_slots = nf > 0 ? slots : 0;
-		D->n_fathers = nf;
-		D->n_children = nf > 0 ? nchild : 0;
-		D->evaluated += nf > 0 ? nchild : 0;
+		D->doom = ub < ub0 ? 1 : 0;
+		D->win = ub < ub0 ? D->win_min : min(D->win_max, 2 * D->win);
 		D->iterations += 1;
+		D->region_len = 0;
+		D->region_slots = 0;
+		D->n_fathers = 0;
+		D->n_children = 0;
 		if (top < 0)
 			D->done = 1;
 	}
 	for (int i = t; i <= n; i += kSelThreads)
 		if (s_hist[i])
 			D->hist[i] += s_hist[i];
+}
+
+// ---- doom: stop expanding under markers the new incumbent condemns ----------
+// One warp walks the top region in DFS order carrying one value: the depth
+// of the condemned marker whose subtree it is inside (or none). An entry at
+// that depth or shallower ends the subtree; entries inside it are marked
+// dead so select never expands them. A marker outside any such subtree
+// whose bound is not below the incumbent opens one. The marker itself is
+// left as it is: commit prunes it when it reaches the top (the sequential
+// search prunes it on take, the incumbent never increases) and drops its
+// whole subtree by depth, including any part beyond this walk.
+__global__ void doom_kernel(ExParams P)
+{
+	ExDev *D = P.dev;
+	if (halted(D) || !D->doom)
+		return;
+	const int lane = threadIdx.x & 31;
+	const long long top = D->top;
+	const int ub = D->ub;
+	const long long stop = max(-1ll, top - P.region_cap);
+	int dd = INT_MAX;         // depth of the open condemned subtree's marker
+	long long dd_at = -1;     // its stack index
+	for (long long base = top; base > stop; base -= 32) {
+		const long long idx = base - lane;
+		Meta e = {0, 0, ST_DEAD, 0};
+		if (idx > stop)
+			e = P.meta[idx];
+		int new_state = -1;
+		for (int k = 0; k < 32; ++k) {
+			const int depth = __shfl_sync(0xffffffffu, int(e.depth), k);
+			const int state = __shfl_sync(0xffffffffu, int(e.state), k);
+			const int lb = __shfl_sync(0xffffffffu, e.lb, k);
+			if (base - k <= stop)
+				break;
+			int ns = -1;
+			if (depth <= dd) {
+				// a condemned subtree seen to its end: settle its marker
+				if (dd != INT_MAX && lane == 0)
+					P.meta[dd_at].state = ST_CONDEMNED;
+				dd = INT_MAX;
+				if (state == ST_BRANCHED && lb >= ub) {
+					dd = depth;
+					dd_at = base - k;
+				}
+			} else {
+				ns = ST_DEAD;
+			}
+			if (lane == k)
+				new_state = ns;
+		}
+		if (new_state >= 0 && idx > stop)
+			P.meta[idx].state = uint8_t(new_state);
+	}
+	// a subtree that runs to the stack bottom also ended inside the walk
+	if (dd != INT_MAX && stop < 0 && lane == 0)
+		P.meta[dd_at].state = ST_CONDEMNED;
+}
+
+// ---- select ---------------------------------------------------------------
+// Chunk c covers region entries [c * kSelChunk, (c + 1) * kSelChunk), region
+// entry r being stack entry top - r.
+__global__ void __launch_bounds__(kSelCtaThreads) select_count_kernel(ExParams P)
+{
+	__shared__ int s_int[32];
+	ExDev *D = P.dev;
+	if (halted(D))
+		return;
+	const long long top = D->top;
+	const int ub = D->ub;
+	const long long scan_len = min(top + 1, P.region_cap);
+	for (int c = blockIdx.x; c < P.n_chunks; c += gridDim.x) {
+		int cand = 0;
+#pragma unroll
+		for (int i = 0; i < kItems; ++i) {
+			const long long r = (long long)c * kSelChunk + kItems * threadIdx.x + i;
+			if (r >= scan_len)
+				break;
+			const long long idx = top - r;
+			const Meta e = P.meta[idx];
+			if (e.state == ST_UNPROC) {
+				if (e.lb >= ub)
+					P.meta[idx].state = ST_PRUNED; // final: the incumbent only decreases
+				else
+					cand++;
+			}
+		}
+		const int total = block_reduce<kSelCtaThreads>(cand, IntSumOp(), 0, s_int);
+		if (threadIdx.x == 0)
+			P.chunk_cnt[c] = total;
+	}
+}
+
+__global__ void __launch_bounds__(kSelThreads) select_plan_kernel(ExParams P)
+{
+	__shared__ long long s_ll[32];
+	ExDev *D = P.dev;
+	if (halted(D))
+		return;
+	long long carry = 0;
+	for (int base = 0; base < P.n_chunks; base += kSelThreads) {
+		const int c = base + threadIdx.x;
+		const long long v = c < P.n_chunks ? P.chunk_cnt[c] : 0;
+		long long tot;
+		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
+		if (c < P.n_chunks)
+			P.chunk_cnt[c] = int(min(carry + ex, (long long)INT_MAX)); // now the chunk base
+		carry += tot;
+	}
+	if (threadIdx.x == 0)
+		D->n_fathers = min(carry, (long long)D->win);
+}
+
+__global__ void __launch_bounds__(kSelCtaThreads) select_write_kernel(ExParams P)
+{
+	__shared__ int s_int[32];
+	ExDev *D = P.dev;
+	if (halted(D))
+		return;
+	const long long top = D->top;
+	const long long nf = D->n_fathers;
+	const int n = P.n;
+	const long long scan_len = min(top + 1, P.region_cap);
+	for (int c = blockIdx.x; c < P.n_chunks; c += gridDim.x) {
+		const long long chunk_base = P.chunk_cnt[c];
+		if ((long long)c * kSelChunk >= scan_len || chunk_base >= nf)
+			continue; // past the region (uniform per CTA)
+		Meta e[kItems];
+		int cand = 0;
+#pragma unroll
+		for (int i = 0; i < kItems; ++i) {
+			const long long r = (long long)c * kSelChunk + kItems * threadIdx.x + i;
+			e[i] = r < scan_len ? P.meta[top - r] : Meta{0, 0, ST_DEAD, 0};
+			cand += e[i].state == ST_UNPROC;
+		}
+		long long order = chunk_base + block_excl_scan<kSelCtaThreads>(cand, IntSumOp(), 0, s_int,
+		                                                                (int *)nullptr);
+#pragma unroll
+		for (int i = 0; i < kItems; ++i) {
+			const long long r = (long long)c * kSelChunk + kItems * threadIdx.x + i;
+			if (r >= scan_len)
+				break;
+			const bool take = e[i].state == ST_UNPROC && order < nf;
+			P.fathers_before[r] = int(min(order, nf));
+			P.father_of[r] = take ? int(order) : -1;
+			if (take) {
+				P.father_ridx[order] = r;
+				P.father_children[order] = children_of_depth(e[i].depth, n);
+				if (order == nf - 1)
+					D->region_len = r + 1;
+			}
+			if (e[i].state == ST_UNPROC)
+				order++;
+		}
+	}
+}
+
+// Child offsets of the fathers (one CTA).
+__global__ void __launch_bounds__(kSelThreads) father_scan_kernel(ExParams P)
+{
+	__shared__ long long s_ll[32];
+	ExDev *D = P.dev;
+	if (halted(D) || D->n_fathers == 0)
+		return;
+	const long long nf = D->n_fathers;
+	long long carry = 0;
+	for (long long base = 0; base < nf; base += kSelThreads) {
+		const long long f = base + threadIdx.x;
+		const long long v = f < nf ? P.father_children[f] : 0;
+		long long tot;
+		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
+		if (f < nf)
+			P.child_off[f] = carry + ex;
+		carry += tot;
+	}
+	if (threadIdx.x == 0) {
+		P.child_off[nf] = carry;
+		D->n_children = carry;
+		D->evaluated += (unsigned long long)carry;
+		D->scanned += (unsigned long long)D->region_len;
+	}
 }
 
 // Copy the region aside and write every father's child records.
@@ -398,9 +626,9 @@ __global__ void make_children_kernel(ExParams P)
 	}
 }
 
-// Per father: choise, ranks, and the rewritten region. One warp per region
-// entry; non-father entries are moved to their new slots.
-__global__ void emit_kernel(ExParams P)
+// Per father (one warp): choise, ranks of the chosen side, and how many of
+// the chosen children the incumbent already prunes.
+__global__ void choose_kernel(ExParams P)
 {
 	ExDev *D = P.dev;
 	if (D->done || D->error || D->n_fathers == 0)
@@ -408,26 +636,13 @@ __global__ void emit_kernel(ExParams P)
 	const int lane = threadIdx.x & 31;
 	const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-	const int S = P.stride, n = P.n;
-	const long long rlen = D->region_len;
-	const long long new_top = D->top - rlen + D->region_slots;
+	const long long nf = D->n_fathers;
 	const int ub = D->ub, best = D->best;
-	for (long long r = warp; r < rlen; r += nwarps) {
-		const long long hi_slot = new_top - P.slot_from_top[r]; // top slot of this block
-		const int f = P.father_of[r];
-		const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
-		if (f < 0) {
-			for (int c = lane; c < S / 16; c += 32)
-				reinterpret_cast<uint4 *>(P.rec + hi_slot * S)[c] = src[c];
-			if (lane == 0)
-				P.meta[hi_slot] = P.tmp_meta[r];
-			continue;
-		}
-		const Meta fm = P.tmp_meta[r];
+	for (long long f = warp; f < nf; f += nwarps) {
 		const long long c0 = P.child_off[f];
 		const int nc = int(P.child_off[f + 1] - c0);
-		const bool simple = fm.depth == n - 2;
-		const int kept = simple ? 2 : nc / 2;
+		const bool simple = nc == 2 && P.tmp_meta[P.father_ridx[f]].depth == P.n - 2;
+		const int kept_all = simple ? 2 : nc / 2;
 		int side_off = 0;
 		if (!simple) {
 			// choise: more children >= best wins; else the larger sum of the
@@ -436,7 +651,7 @@ __global__ void emit_kernel(ExParams P)
 			int cut[2] = {0, 0};
 			for (int k = lane; k < nc; k += 32) {
 				const int lb = P.child_lb[c0 + k];
-				const int sd = k >= kept;
+				const int sd = k >= kept_all;
 				if (lb >= best)
 					cut[sd]++;
 				else
@@ -449,59 +664,132 @@ __global__ void emit_kernel(ExParams P)
 				cut[0] += __shfl_xor_sync(0xffffffffu, cut[0], d);
 				cut[1] += __shfl_xor_sync(0xffffffffu, cut[1], d);
 			}
-			bool begin;
-			if (cut[0] != cut[1])
-				begin = cut[0] > cut[1];
-			else
-				begin = sum[0] > sum[1];
-			side_off = begin ? 0 : kept;
+			const bool begin = cut[0] != cut[1] ? cut[0] > cut[1] : sum[0] > sum[1];
+			side_off = begin ? 0 : kept_all;
 		}
-		// ranks: 0 = smallest bound, ties to the smaller job; rank 0 sits
-		// right under the marker
-		for (int k = lane; k < kept; k += 32) {
+		// rank 0 = smallest bound, ties to the smaller job (select_worst)
+		int open = 0;
+		for (int k = lane; k < kept_all; k += 32) {
 			const long long ck = c0 + side_off + k;
 			const int lb = P.child_lb[ck];
 			const int job = P.child_job[ck];
 			int rank = 0;
-			for (int q = 0; q < kept; ++q) {
+			for (int q = 0; q < kept_all; ++q) {
 				const int lq = P.child_lb[c0 + side_off + q];
 				const int jq = P.child_job[c0 + side_off + q];
 				rank += (lq < lb) || (lq == lb && jq < job);
 			}
+			P.child_rank[ck] = rank;
+			open += (simple || lb < ub) ? 1 : 0;
+		}
+#pragma unroll
+		for (int d = 16; d > 0; d >>= 1)
+			open += __shfl_xor_sync(0xffffffffu, open, d);
+		if (lane == 0) {
+			P.father_side[f] = side_off;
+			P.father_kept[f] = open;
+			P.father_npr[f] = kept_all - open;
+		}
+	}
+}
+
+// Block sizes of the fathers in the rewritten region (one CTA).
+__global__ void __launch_bounds__(kSelThreads) kept_scan_kernel(ExParams P)
+{
+	__shared__ long long s_ll[32];
+	ExDev *D = P.dev;
+	if (halted(D) || D->n_fathers == 0)
+		return;
+	const long long nf = D->n_fathers;
+	long long carry = 0;
+	for (long long base = 0; base < nf; base += kSelThreads) {
+		const long long f = base + threadIdx.x;
+		const long long v = f < nf ? 1 + P.father_kept[f] : 0;
+		long long tot;
+		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
+		if (f < nf)
+			P.kept_before[f] = carry + ex;
+		carry += tot;
+	}
+	if (threadIdx.x == 0) {
+		P.kept_before[nf] = carry;
+		const long long slots = (D->region_len - nf) + carry;
+		const long long new_top = D->top - D->region_len + slots;
+		if (new_top >= P.cap) {
+			D->error = WSBB_ERR_CAPACITY;
+			D->n_fathers = 0;
+			D->region_len = 0;
+		}
+		D->region_slots = slots;
+	}
+}
+
+// Scatter the rewritten region: one warp per region entry. Region entry r
+// has r - fb non-father entries above it (one slot each) and fb father
+// blocks (kept_before[fb] slots), fb = fathers above it.
+__global__ void emit_kernel(ExParams P)
+{
+	ExDev *D = P.dev;
+	if (halted(D) || D->n_fathers == 0)
+		return;
+	const int lane = threadIdx.x & 31;
+	const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+	const int S = P.stride, n = P.n;
+	const long long rlen = D->region_len;
+	const long long new_top = D->top - rlen + D->region_slots;
+	for (long long r = warp; r < rlen; r += nwarps) {
+		const int fb = P.fathers_before[r];
+		const long long hi_slot = new_top - ((r - fb) + P.kept_before[fb]);
+		const int f = P.father_of[r];
+		const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
+		for (int c = lane; c < S / 16; c += 32)
+			reinterpret_cast<uint4 *>(P.rec + hi_slot * S)[c] = src[c];
+		if (f < 0) {
+			if (lane == 0)
+				P.meta[hi_slot] = P.tmp_meta[r];
+			continue;
+		}
+		const Meta fm = P.tmp_meta[r];
+		const bool simple = fm.depth == n - 2;
+		const long long c0 = P.child_off[f] + P.father_side[f];
+		const int kept_all = simple ? 2 : int(P.child_off[f + 1] - P.child_off[f]) / 2;
+		const int open = P.father_kept[f];
+		for (int k = lane; k < kept_all; k += 32) {
+			const long long ck = c0 + k;
+			const int rank = P.child_rank[ck];
+			if (rank >= open)
+				continue; // pruned at birth: counted with the marker
 			const long long slot = hi_slot - 1 - rank;
 			const uint4 *cs = reinterpret_cast<const uint4 *>(P.child_rec + ck * S);
 			uint4 *dst = reinterpret_cast<uint4 *>(P.rec + slot * S);
 			for (int c = 0; c < S / 16; ++c)
 				dst[c] = cs[c];
 			Meta cm;
-			cm.lb = lb;
-			cm.depth = int16_t(simple ? n : fm.depth + 1);
-			cm.state = simple ? ST_LEAF : (lb >= ub ? ST_PRUNED : ST_UNPROC);
-			cm.pad = 0;
+			cm.lb = P.child_lb[ck];
+			cm.depth = uint8_t(simple ? n : fm.depth + 1);
+			cm.state = simple ? ST_LEAF : ST_UNPROC;
+			cm.npruned = 0;
 			P.meta[slot] = cm;
 		}
-		for (int c = lane; c < S / 16; c += 32)
-			reinterpret_cast<uint4 *>(P.rec + hi_slot * S)[c] = src[c];
 		if (lane == 0) {
 			Meta mm = fm;
 			mm.state = ST_BRANCHED;
+			mm.npruned = uint16_t(P.father_npr[f]);
 			P.meta[hi_slot] = mm;
 		}
 	}
-	__syncthreads();
 }
 
 __global__ void finish_iteration_kernel(ExParams P)
 {
 	ExDev *D = P.dev;
-	if (D->done || D->error || D->n_fathers == 0)
+	if (halted(D) || D->n_fathers == 0)
 		return;
 	D->top = D->top - D->region_len + D->region_slots;
-	D->n_fathers = 0;
-	D->n_children = 0;
 }
 
-__global__ void init_kernel(ExParams P, int ub0, int best)
+__global__ void init_kernel(ExParams P, int ub0, int best, int win_min, int win_max)
 {
 	ExDev *D = P.dev;
 	const int n = P.n, S = P.stride;
@@ -510,6 +798,9 @@ __global__ void init_kernel(ExParams P, int ub0, int best)
 		D->top = 0;
 		D->ub = ub0;
 		D->best = best;
+		D->win = win_min;
+		D->win_min = win_min;
+		D->win_max = win_max;
 		Meta m0 = {0, 0, ST_UNPROC, 0};
 		P.meta[0] = m0;
 	}
@@ -525,6 +816,49 @@ __global__ void init_kernel(ExParams P, int ub0, int best)
 		r[j] = v;
 		reinterpret_cast<int16_t *>(P.best_rec)[j] = int16_t(j < n ? -1 : 0);
 	}
+}
+
+// Lays the search buffers out from `base` (null: only sizes them).
+size_t search_layout(uint8_t *base, long long cap, long long region_cap, int window, int n,
+                     int S, ExParams &P)
+{
+	const long long child_cap = (long long)window * 2 * n;
+	const int n_chunks = int((region_cap + kSelChunk - 1) / kSelChunk);
+	auto a256 = [](size_t v) { return (v + 255) & ~size_t(255); };
+	size_t off = 0;
+	auto take = [&](size_t bytes) {
+		const size_t at = off;
+		off = a256(off + bytes);
+		return base ? base + at : nullptr;
+	};
+	P.dev = reinterpret_cast<ExDev *>(take(sizeof(ExDev)));
+	P.rec = take(size_t(cap) * S);
+	P.meta = reinterpret_cast<Meta *>(take(size_t(cap) * sizeof(Meta)));
+	P.tmp_rec = take(size_t(region_cap) * S);
+	P.tmp_meta = reinterpret_cast<Meta *>(take(size_t(region_cap) * sizeof(Meta)));
+	P.fathers_before = reinterpret_cast<int *>(take(size_t(region_cap) * 4));
+	P.father_of = reinterpret_cast<int *>(take(size_t(region_cap) * 4));
+	P.chunk_cnt = reinterpret_cast<int *>(take(size_t(n_chunks) * 4));
+	P.father_ridx = reinterpret_cast<long long *>(take(size_t(window) * 8));
+	P.child_off = reinterpret_cast<long long *>(take(size_t(window + 1) * 8));
+	P.father_children = reinterpret_cast<int *>(take(size_t(window) * 4));
+	P.father_side = reinterpret_cast<int *>(take(size_t(window) * 4));
+	P.father_kept = reinterpret_cast<int *>(take(size_t(window) * 4));
+	P.father_npr = reinterpret_cast<int *>(take(size_t(window) * 4));
+	P.kept_before = reinterpret_cast<long long *>(take(size_t(window + 1) * 8));
+	P.child_rec = take(size_t(child_cap) * S);
+	P.child_lb = reinterpret_cast<int32_t *>(take(size_t(child_cap) * 4));
+	P.child_job = reinterpret_cast<int16_t *>(take(size_t(child_cap) * 2));
+	P.child_rank = reinterpret_cast<int32_t *>(take(size_t(child_cap) * 4));
+	P.best_rec = take(size_t(S));
+	P.cap = cap;
+	P.region_cap = region_cap;
+	P.child_cap = child_cap;
+	P.window = window;
+	P.n_chunks = n_chunks;
+	P.n = n;
+	P.stride = S;
+	return off;
 }
 
 }  // namespace
@@ -561,20 +895,56 @@ int ex_fail(wsbb_ctx *ctx, cudaError_t e, const char *what)
 	return wsbb_set_error(ctx, WSBB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// One iteration: four stream-ordered launches (captured into a graph).
+// One iteration: a fixed sequence of stream-ordered launches (captured
+// into a graph).
 cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 {
 	using namespace wsbb;
-	commit_select_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	const int grid = ctx->num_sms * 4;
+	const int sel_grid = std::min(X.P.n_chunks, ctx->num_sms * 8);
+	commit_kernel<<<1, kSelThreads, 0, s>>>(X.P);
+	doom_kernel<<<1, 32, 0, s>>>(X.P);
+	select_count_kernel<<<sel_grid, kSelCtaThreads, 0, s>>>(X.P);
+	select_plan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
+	select_write_kernel<<<sel_grid, kSelCtaThreads, 0, s>>>(X.P);
+	father_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	make_children_kernel<<<grid, 256, 0, s>>>(X.P);
 	cudaError_t e = launch_pool_bounds(X.child_bp, X.P.child_rec, X.child_cap, X.P.child_lb, 0,
 	                                   ctx->num_sms, s);
 	if (e != cudaSuccess)
 		return e;
+	choose_kernel<<<grid, 256, 0, s>>>(X.P);
+	kept_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	emit_kernel<<<grid, 256, 0, s>>>(X.P);
 	finish_iteration_kernel<<<1, 32, 0, s>>>(X.P);
 	return cudaGetLastError();
+}
+
+// Window bounds: at most `window` fathers per iteration, shrinking to
+// window / 64 (at least 64) after an incumbent improvement.
+int window_min_of(int window) { return std::min(window, std::max(64, window / 64)); }
+
+void fill_stats(const wsbb::ExDev &h, const int16_t *best_rec, int n, int status,
+                double seconds, wsbb_stats *st)
+{
+	std::memset(st, 0, sizeof(*st));
+	st->branched = (int64_t)h.branched;
+	st->pruned = (int64_t)h.pruned;
+	st->leaves = (int64_t)h.leaves;
+	st->improved = (int64_t)h.improved;
+	st->bounded = (int64_t)h.bounded;
+	st->evaluated = (int64_t)h.evaluated;
+	st->discarded = (int64_t)h.discarded;
+	st->iterations = (int64_t)h.iterations;
+	st->best_cost = h.ub;
+	st->status = h.error ? h.error : status;
+	for (int d = 0; d <= n; ++d)
+		st->depth_hist[d] = h.hist[d];
+	for (int j = 0; j < n; ++j)
+		st->best_perm[j] = best_rec[j];
+	st->seconds = seconds;
+	st->scanned = (int64_t)h.scanned;
+	st->committed = (int64_t)h.committed;
 }
 
 }  // namespace
@@ -589,11 +959,22 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "cudaSetDevice");
 	const int n = ctx->inst.n;
-	const int window = cfg->window > 0 ? cfg->window : 4096;
-	const long long cap = cfg->capacity > 0 ? cfg->capacity : (1ll << 22);
-	const long long region_cap = 4ll * window + 4096;
-	const long long child_cap = (long long)window * 2 * n;
 	const int S = ctx->bp.stride;
+	const int window = cfg->window > 0 ? cfg->window : 16384;
+	long long cap = cfg->capacity;
+	if (cap <= 0) {
+		// A `window`-wide DFS keeps up to about window * u entries per level
+		// live: 2 * window * n^2 covers it, within half the free memory.
+		cap = std::max(1ll << 22, 2ll * window * n * n);
+		size_t free_b = 0, total_b = 0;
+		if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+			const long long fit = (long long)(free_b / 2 / (S + sizeof(Meta)));
+			cap = std::min(cap, std::max(fit, 1ll << 20));
+		}
+	}
+	// Scanning past pruned entries to fill the window is cheap next to an
+	// under-filled iteration; the region copy grows with it.
+	const long long region_cap = 16ll * window + 8192;
 	if (window > (1 << 20) || cap < region_cap)
 		return wsbb_set_error(ctx, WSBB_ERR_ARG, "window / capacity out of range");
 
@@ -601,61 +982,24 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 	if (!X || X->cap != cap || X->window != window) {
 		wsbb_explore_release(ctx);
 		X = new ExploreState();
-		X->cap = cap;
-		X->region_cap = region_cap;
-		X->child_cap = child_cap;
-		X->window = window;
-		auto a16 = [](size_t v) { return (v + 255) & ~size_t(255); };
-		size_t off = 0;
-		const size_t o_dev = off; off = a16(off + sizeof(ExDev));
-		const size_t o_rec = off; off = a16(off + size_t(cap) * S);
-		const size_t o_meta = off; off = a16(off + size_t(cap) * sizeof(Meta));
-		const size_t o_trec = off; off = a16(off + size_t(region_cap) * S);
-		const size_t o_tmeta = off; off = a16(off + size_t(region_cap) * sizeof(Meta));
-		const size_t o_sft = off; off = a16(off + size_t(region_cap) * 8);
-		const size_t o_fof = off; off = a16(off + size_t(region_cap) * 4);
-		const size_t o_fr = off; off = a16(off + size_t(window) * 8);
-		const size_t o_co = off; off = a16(off + size_t(window + 1) * 8);
-		const size_t o_crec = off; off = a16(off + size_t(child_cap) * S);
-		const size_t o_clb = off; off = a16(off + size_t(child_cap) * 4);
-		const size_t o_cjob = off; off = a16(off + size_t(child_cap) * 2);
-		const size_t o_best = off; off = a16(off + size_t(S));
-		X->bytes = off;
+		X->bytes = search_layout(nullptr, cap, region_cap, window, n, S, X->P);
 		e = cudaMalloc(&X->mem, X->bytes);
 		if (e != cudaSuccess) {
 			delete X;
 			return wsbb_set_error(ctx, WSBB_ERR_NOMEM, "search pool allocation failed");
 		}
-		uint8_t *b = static_cast<uint8_t *>(X->mem);
-		ExParams &P = X->P;
-		P.dev = reinterpret_cast<ExDev *>(b + o_dev);
-		P.rec = b + o_rec;
-		P.meta = reinterpret_cast<Meta *>(b + o_meta);
-		P.tmp_rec = b + o_trec;
-		P.tmp_meta = reinterpret_cast<Meta *>(b + o_tmeta);
-		P.slot_from_top = reinterpret_cast<long long *>(b + o_sft);
-		P.father_of = reinterpret_cast<int *>(b + o_fof);
-		P.father_ridx = reinterpret_cast<long long *>(b + o_fr);
-		P.child_off = reinterpret_cast<long long *>(b + o_co);
-		P.child_rec = b + o_crec;
-		P.child_lb = reinterpret_cast<int32_t *>(b + o_clb);
-		P.child_job = reinterpret_cast<int16_t *>(b + o_cjob);
-		P.best_rec = b + o_best;
-		P.cap = cap;
-		P.region_cap = region_cap;
-		P.child_cap = child_cap;
-		P.window = window;
-		P.n = n;
-		P.stride = S;
+		search_layout(static_cast<uint8_t *>(X->mem), cap, region_cap, window, n, S, X->P);
+		X->cap = cap;
+		X->region_cap = region_cap;
+		X->child_cap = X->P.child_cap;
+		X->window = window;
 		X->child_bp = ctx->bp;
-		X->child_bp.count_dev = &P.dev->n_children;
+		X->child_bp.count_dev = &X->P.dev->n_children;
 		ctx->ex = X;
 	}
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
-	const int ub0 = cfg->ub0;
-	const int best = cfg->best;
-	init_kernel<<<1, 128, 0, s>>>(X->P, ub0, best);
+	init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window);
 	e = cudaGetLastError();
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "search init");
@@ -724,23 +1068,7 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 	e = cudaMemcpy(best_rec.data(), X->P.best_rec, S, cudaMemcpyDeviceToHost);
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "incumbent download");
-
-	std::memset(st, 0, sizeof(*st));
-	st->branched = (int64_t)h.branched;
-	st->pruned = (int64_t)h.pruned;
-	st->leaves = (int64_t)h.leaves;
-	st->improved = (int64_t)h.improved;
-	st->bounded = (int64_t)h.bounded;
-	st->evaluated = (int64_t)h.evaluated;
-	st->discarded = (int64_t)h.discarded;
-	st->iterations = (int64_t)h.iterations;
-	st->best_cost = h.ub;
-	st->status = h.error ? h.error : status;
-	for (int d = 0; d <= n; ++d)
-		st->depth_hist[d] = h.hist[d];
-	for (int j = 0; j < n; ++j)
-		st->best_perm[j] = best_rec[j];
-	st->seconds = ms * 1e-3;
+	fill_stats(h, best_rec.data(), n, status, ms * 1e-3, st);
 	if (h.error)
 		return wsbb_set_error(ctx, h.error, "search pool capacity exceeded");
 	return WSBB_OK;
@@ -779,43 +1107,6 @@ int noalloc_scratch(wsbb_ctx *ctx, uint8_t **out)
 	return WSBB_OK;
 }
 
-// Lays the search buffers out from `base` (null: only sizes them).
-size_t noalloc_layout(uint8_t *base, long long cap, int window, int n, int S,
-                      wsbb::ExParams &P)
-{
-	using wsbb::ExDev;
-	using wsbb::Meta;
-	const long long region_cap = 4ll * window + 4096;
-	const long long child_cap = (long long)window * 2 * n;
-	auto a256 = [](size_t v) { return (v + 255) & ~size_t(255); };
-	size_t off = 0;
-	auto take = [&](size_t bytes) {
-		const size_t at = off;
-		off = a256(off + bytes);
-		return base ? base + at : nullptr;
-	};
-	P.dev = reinterpret_cast<ExDev *>(take(sizeof(ExDev)));
-	P.rec = take(size_t(cap) * S);
-	P.meta = reinterpret_cast<Meta *>(take(size_t(cap) * sizeof(Meta)));
-	P.tmp_rec = take(size_t(region_cap) * S);
-	P.tmp_meta = reinterpret_cast<Meta *>(take(size_t(region_cap) * sizeof(Meta)));
-	P.slot_from_top = reinterpret_cast<long long *>(take(size_t(region_cap) * 8));
-	P.father_of = reinterpret_cast<int *>(take(size_t(region_cap) * 4));
-	P.father_ridx = reinterpret_cast<long long *>(take(size_t(window) * 8));
-	P.child_off = reinterpret_cast<long long *>(take(size_t(window + 1) * 8));
-	P.child_rec = take(size_t(child_cap) * S);
-	P.child_lb = reinterpret_cast<int32_t *>(take(size_t(child_cap) * 4));
-	P.child_job = reinterpret_cast<int16_t *>(take(size_t(child_cap) * 2));
-	P.best_rec = take(size_t(S));
-	P.cap = cap;
-	P.region_cap = region_cap;
-	P.child_cap = child_cap;
-	P.window = window;
-	P.n = n;
-	P.stride = S;
-	return off;
-}
-
 }  // namespace
 
 extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
@@ -839,19 +1130,19 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	ExploreState X; // host-side view only: no graph, no allocation
 	if (window > (1 << 20))
 		return wsbb_set_error(ctx, WSBB_ERR_ARG, "window out of range");
+	const long long region_cap = 4ll * window + 4096;
 	long long cap = cfg->capacity;
 	if (cap <= 0) {
-		const size_t fixed = noalloc_layout(nullptr, 0, window, n, S, X.P);
+		const size_t fixed = search_layout(nullptr, 0, region_cap, window, n, S, X.P);
 		cap = fixed < limit ? (long long)((limit - fixed) / (S + sizeof(Meta))) : 0;
-		while (cap > 0 && noalloc_layout(nullptr, cap, window, n, S, X.P) > limit)
+		while (cap > 0 && search_layout(nullptr, cap, region_cap, window, n, S, X.P) > limit)
 			cap -= 256;
 	}
-	const long long region_cap = 4ll * window + 4096;
-	if (cap < region_cap || noalloc_layout(nullptr, cap, window, n, S, X.P) > limit)
+	if (cap < region_cap || search_layout(nullptr, cap, region_cap, window, n, S, X.P) > limit)
 		return wsbb_set_error(ctx, WSBB_ERR_CAPACITY,
 		                      "window / capacity do not fit the fixed no-alloc scratch of " +
 		                          std::to_string(limit >> 20) + " MiB");
-	noalloc_layout(scratch, cap, window, n, S, X.P);
+	search_layout(scratch, cap, region_cap, window, n, S, X.P);
 	X.cap = cap;
 	X.region_cap = region_cap;
 	X.child_cap = X.P.child_cap;
@@ -861,7 +1152,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
 	const auto t0 = std::chrono::steady_clock::now();
-	init_kernel<<<1, 128, 0, s>>>(X.P, cfg->ub0, cfg->best);
+	init_kernel<<<1, 128, 0, s>>>(X.P, cfg->ub0, cfg->best, window_min_of(window), window);
 	e = cudaGetLastError();
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "search init");
@@ -896,23 +1187,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 		return ex_fail(ctx, e, "incumbent download");
 	const double secs =
 	    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-
-	std::memset(st, 0, sizeof(*st));
-	st->branched = (int64_t)h.branched;
-	st->pruned = (int64_t)h.pruned;
-	st->leaves = (int64_t)h.leaves;
-	st->improved = (int64_t)h.improved;
-	st->bounded = (int64_t)h.bounded;
-	st->evaluated = (int64_t)h.evaluated;
-	st->discarded = (int64_t)h.discarded;
-	st->iterations = (int64_t)h.iterations;
-	st->best_cost = h.ub;
-	st->status = h.error ? h.error : status;
-	for (int d = 0; d <= n; ++d)
-		st->depth_hist[d] = h.hist[d];
-	for (int j = 0; j < n; ++j)
-		st->best_perm[j] = best_rec[j];
-	st->seconds = secs;
+	fill_stats(h, best_rec, n, status, secs, st);
 	if (h.error)
 		return wsbb_set_error(ctx, h.error, "search outgrew the no-alloc scratch capacity");
 	return WSBB_OK;

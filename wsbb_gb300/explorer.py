@@ -30,7 +30,8 @@ class ExploreStats(C.Structure):
                 ("improved", C.c_int64), ("bounded", C.c_int64), ("evaluated", C.c_int64),
                 ("discarded", C.c_int64), ("iterations", C.c_int64), ("best_cost", C.c_int32),
                 ("status", C.c_int32), ("depth_hist", C.c_uint64 * (MAX_JOBS + 1)),
-                ("best_perm", C.c_int32 * MAX_JOBS), ("seconds", C.c_double)]
+                ("best_perm", C.c_int32 * MAX_JOBS), ("seconds", C.c_double),
+                ("scanned", C.c_int64), ("committed", C.c_int64)]
 
 
 NO_GRAPH = 1
@@ -59,4 +60,4 @@ def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int
             "best_cost": st.best_cost, "status": st.status,
             "coverage": coverage(st.depth_hist, n),
             "best_perm": np.array(st.best_perm[:n], dtype=np.int32),
-            "seconds": st.seconds}
+            "seconds": st.seconds, "scanned": st.scanned, "committed": st.committed}
