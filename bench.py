@@ -128,6 +128,51 @@ def cpu_port_rate(nthreads: int, count: int, seed: int = 0) -> tuple[float, dict
                                   f"{nthreads} host threads, {dt:.2f} s"}
 
 
+SEARCH_N, SEARCH_M, SEARCH_SEEDS = 50, 10, (0, 1, 2, 3, 4)
+
+
+def cpu_search_rate(seconds: float = 10.0) -> dict:
+    """The oracle's sequential search (the reference CPU explorer's
+    semantics, single-threaded like one reference peer) on the first search
+    instance, capped by node count: bounded nodes per second."""
+    from oracle import oracle as O
+    p = O.gen_instance(SEARCH_SEEDS[0], SEARCH_N, SEARCH_M)
+    ub, _ = O.neh(p)
+    b = O.Bound(p)
+    cap = 2000
+    while True:
+        t0 = time.perf_counter()
+        rc, st, _ = b.explore(ub0=ub, node_cap=cap)
+        dt = time.perf_counter() - t0
+        if dt > seconds / 4 or rc == 0:
+            break
+        cap *= 4
+    return {"value": st["bounded"] / dt, "unit": "bounded nodes/s", "cores": 1, "kind": "port",
+            "sample": f"first {cap} takes of the n={SEARCH_N} m={SEARCH_M} seed-"
+                      f"{SEARCH_SEEDS[0]} search, {dt:.1f} s"}
+
+
+def search_section(cpu: bool) -> dict:
+    """Time-to-proof of the exact GPU search on the persistent-explorer
+    instances (n=50, m=10, seeds 0-4, NEH incumbent)."""
+    from wsbb_gb300 import search_bench
+    out = search_bench.run(SEARCH_N, SEARCH_M, SEARCH_SEEDS, verbose=False)
+    sec = {"workload": f"exact DFS time-to-proof, n={SEARCH_N} m={SEARCH_M}, seeds "
+                       f"{list(SEARCH_SEEDS)}, NEH initial incumbent, best=99999; tree "
+                       "identical to the reference CPU search",
+           "all_proved": out["all_proved"], "time_to_proof_s": out["seconds"],
+           "bounded_nodes": out["bounded"], "bounded_nodes_per_s": out["bounded_per_s"],
+           "evaluated_bounds": out["evaluated"],
+           "per_instance": [{k: r[k] for k in ("seed", "optimum", "branched", "pruned",
+                                               "leaves", "bounded", "seconds")}
+                            for r in out["runs"]]}
+    if cpu:
+        c = cpu_search_rate()
+        sec["cpu_baseline"] = c
+        sec["cpu_est_time_to_proof_s"] = out["bounded"] / c["value"]
+    return sec
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -243,6 +288,9 @@ def run_gpu(args) -> None:
         e2e_s = float(t.item())
     e2e_value = world * e2e_steps * POOL / e2e_s
 
+    search = None
+    if not args.no_search:
+        search = search_section(cpu=(rank == 0 and world == 1))
     if rank == 0:
         cpu = None
         if world == 1:
@@ -282,6 +330,7 @@ def run_gpu(args) -> None:
             "clocks": clk.summary(),
             "gpu_launches": args.steps,
             "wall_s_timed": t_wall,
+            "search": search,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -294,6 +343,8 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="wsbb", choices=["wsbb", "reference"])
+    ap.add_argument("--no-search", action="store_true",
+                    help="skip the time-to-proof section (search workload)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -150,6 +150,7 @@ typedef struct {
 	double seconds;     /* device time of the search */
 	int64_t scanned;    /* stack entries scanned to select fathers */
 	int64_t committed;  /* stack entries committed */
+	int64_t early;      /* children settled by the learned K-pair test */
 } wsbb_stats;
 
 int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
@@ -184,6 +185,66 @@ int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
 #define WSBB_NOALLOC_SCRATCH_BYTES (24u << 20)
 int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
                          wsbb_stats *stats, void *stream);
+
+/*
+ * Learned machine-pair selector (no counterpart in the reference: the
+ * reference only counts binding pairs, nbFois at src/bound_flowshop.cpp:157,
+ * and its pair re-ordering is commented out, :129-130).
+ *
+ * A 3-layer MLP (D -> 128 -> 128 -> P, ReLU, bf16 operands, fp32
+ * accumulation) maps a node's features — effective heads and tails per
+ * machine divided by the largest machine load, and the free-job mask;
+ * D = round_up(2m + n, 16) — to scores of the P machine pairs. Trained on
+ * the GPU (Adam, softmax cross-entropy against the node's binding pair).
+ * In a search it ranks, per father, the K pairs tried first on all of its
+ * children; a child whose bound over those K pairs already reaches
+ * max(best, incumbent) is settled without the other pairs. That leaves
+ * the tree unchanged: such a child is pruned at birth either way and only
+ * counts (never sums) in the side choice. With the reference default
+ * best = 99999 nothing can be settled (the side choice sums every child's
+ * exact bound), so the learned search is run with best = the initial
+ * incumbent, and compared with the plain search at the same `best`.
+ */
+typedef struct wsbb_model wsbb_model;
+
+int wsbb_model_create(int n, int m, uint64_t seed, wsbb_model **out); /* m <= 20 */
+void wsbb_model_destroy(wsbb_model *model);
+const char *wsbb_model_last_error(const wsbb_model *model);
+int wsbb_model_dims(const wsbb_model *model, int *D, int *O, int64_t *nparams);
+/* fp32 weights W1[D][128], b1, W2[128][128], b2, W3[128][O], b3 (O =
+ * round_up(P, 8); columns >= P are padding) */
+int wsbb_model_get_weights(const wsbb_model *model, float *host, int64_t count);
+int wsbb_model_set_weights(wsbb_model *model, const float *host, int64_t count);
+/* re-derive the bf16 inference weights after the fp32 ones changed */
+int wsbb_model_pack(wsbb_model *model);
+
+/* Features (rows of D floats, device) and, when `labels` is not NULL, the
+ * binding pair of each record (-1 for leaves), for device records. */
+float wsbb_feature_scale(const wsbb_ctx *ctx);
+int wsbb_features(wsbb_ctx *ctx, const void *recs, int64_t count, float inv_scale, int D,
+                  float *X, int32_t *labels, void *stream);
+/* One forward/backward pass over B device rows: fp32 gradients (host,
+ * nparams floats) and the summed loss (host). Synchronous. */
+int wsbb_model_grads(wsbb_model *model, const float *X, const int32_t *y, int B,
+                     float *grad_host, float *loss_host);
+/* Adam training over `count` device rows; mean loss per epoch to host. */
+int wsbb_model_train(wsbb_model *model, const float *X, const int32_t *y, int64_t count,
+                     int epochs, int batch, float lr, uint64_t seed, float *epoch_loss_host);
+/* Inference: top-K pair indices per row (device, best first) and,
+ * optionally, the O logits per row (device). */
+int wsbb_model_topk(wsbb_model *model, const float *X, int64_t rows, int K, int16_t *topk,
+                    float *logits, void *stream);
+
+/* The search of wsbb_explore with the learned K-pair test ahead of LB2
+ * (1 <= K <= 32). Same counters as wsbb_explore with the same cfg;
+ * stats->early counts children settled by the K pairs. */
+int wsbb_explore_learned(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_model *model, int K,
+                         wsbb_stats *stats, void *stream);
+/* The plain search, also copying a sample of the bounded children (every
+ * `stride`-th, hashed per iteration) into `recs_out` (device, `cap`
+ * records); *logged receives how many were written. Training data. */
+int wsbb_explore_log(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, void *recs_out, int64_t cap,
+                     int stride, int64_t *logged, wsbb_stats *stats, void *stream);
 
 /* Measured integer max-plus issue rate of `device` (add + max operations
  * per second over every SM): the denominator of the LB2 kernel's

@@ -92,18 +92,21 @@ __device__ __forceinline__ Staged stage_tables(const TableView &tv, uint8_t *sme
 
 __host__ __device__ __forceinline__ int rec_words_of(int stride) { return (stride / 4) | 1; }
 
-// Copy records [base, base + nrec) of the pool into this warp's staging rows
-// (odd word stride: lanes reading their own row hit distinct banks).
+// Copy records [base, base + nrec) of the pool — or, with `gather`, the
+// records gather[base..base + nrec) — into this warp's staging rows (odd
+// word stride: lanes reading their own row hit distinct banks).
 __device__ __forceinline__ void stage_records(int stride, const uint8_t *recs, int64_t base,
-                                              int nrec, uint32_t *rows, int rec_words, int lane)
+                                              int nrec, uint32_t *rows, int rec_words, int lane,
+                                              const int32_t *gather)
 {
 	const int chunks_per_rec = stride / 16;
-	const uint4 *src = reinterpret_cast<const uint4 *>(recs + base * stride);
 	const int nchunks = nrec * chunks_per_rec;
 	for (int c = lane; c < nchunks; c += 32) {
-		const uint4 v = __ldg(src + c);
 		const int r = c / chunks_per_rec;
-		uint32_t *d = rows + r * rec_words + (c - r * chunks_per_rec) * 4;
+		const int k = c - r * chunks_per_rec;
+		const int64_t rid = gather ? int64_t(gather[base + r]) : base + r;
+		const uint4 v = __ldg(reinterpret_cast<const uint4 *>(recs + rid * stride) + k);
+		uint32_t *d = rows + r * rec_words + k * 4;
 		d[0] = v.x;
 		d[1] = v.y;
 		d[2] = v.z;
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(kFastThreads, 2)
 	for (int64_t base = (int64_t(blockIdx.x) * kFastWarps + warp) * 32; base < count;
 	     base += step) {
 		const int nrec = count - base < 32 ? int(count - base) : 32;
-		stage_records(bp.stride, recs, base, nrec, rows, rec_words, lane);
+		stage_records(bp.stride, recs, base, nrec, rows, rec_words, lane, bp.gather);
 		__syncwarp();
 		bool work = false;
 		int32_t lb = 0;
@@ -287,7 +290,7 @@ __global__ void __launch_bounds__(kFastThreads, 2)
 			}
 		}
 		if (lane < nrec)
-			out[base + lane] = lb;
+			out[bp.gather ? int64_t(bp.gather[base + lane]) : base + lane] = lb;
 		__syncwarp(); // the next batch's staging overwrites the columns
 	}
 }
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(kThreads) lb2_pool_kernel(BoundParams bp,
 	for (int64_t base = (int64_t(blockIdx.x) * kWarps + warp) * 32; base < count;
 	     base += step) {
 		const int nrec = count - base < 32 ? int(count - base) : 32;
-		stage_records(bp.stride, recs, base, nrec, rows, rec_words, lane);
+		stage_records(bp.stride, recs, base, nrec, rows, rec_words, lane, bp.gather);
 		__syncwarp();
 		if (lane < nrec) {
 			const int16_t *rec = reinterpret_cast<const int16_t *>(rows + lane * rec_words);
@@ -385,7 +388,7 @@ __global__ void __launch_bounds__(kThreads) lb2_pool_kernel(BoundParams bp,
 					lb = imax(lb, v1);
 				}
 			}
-			out[base + lane] = lb;
+			out[bp.gather ? int64_t(bp.gather[base + lane]) : base + lane] = lb;
 		}
 		__syncwarp();
 	}
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) aux_pool_kernel(BoundParams bp,
 	for (int64_t base = (int64_t(blockIdx.x) * kWarps + warp) * 32; base < count;
 	     base += step) {
 		const int nrec = count - base < 32 ? int(count - base) : 32;
-		stage_records(bp.stride, recs, base, nrec, rows, rec_words, lane);
+		stage_records(bp.stride, recs, base, nrec, rows, rec_words, lane, bp.gather);
 		__syncwarp();
 		if (lane < nrec) {
 			const int16_t *rec = reinterpret_cast<const int16_t *>(rows + lane * rec_words);
@@ -442,7 +445,7 @@ __global__ void __launch_bounds__(kThreads) aux_pool_kernel(BoundParams bp,
 					res = imax(res, head + work + tail);
 				}
 			}
-			out[base + lane] = res;
+			out[bp.gather ? int64_t(bp.gather[base + lane]) : base + lane] = res;
 		}
 		__syncwarp();
 	}

@@ -64,6 +64,7 @@
 #include <mutex>
 #include <string>
 
+#include "node_features.cuh"
 #include "wsbb_internal.h"
 
 namespace wsbb {
@@ -100,6 +101,9 @@ struct ExDev {
 	int win, win_min, win_max, doom;
 	unsigned long long branched, pruned, leaves, improved, bounded;
 	unsigned long long evaluated, discarded, scanned, committed;
+	unsigned long long early;      // children settled by the learned K-pair test
+	long long n_unsettled;         // children left for full LB2 this iteration
+	unsigned long long log_count;  // training records written
 	unsigned long long hist[WSBB_MAX_JOBS + 1];
 };
 
@@ -127,6 +131,16 @@ struct ExParams {
 	long long cap, region_cap, child_cap;
 	int window;               // maximum fathers per iteration
 	int n_chunks;             // select chunks covering region_cap
+	// learned mode
+	float *feat;              // [window][D] father features
+	int16_t *fpairs;          // [window][K] pairs ranked by the selector
+	int32_t *unsettled;       // [child_cap] children left for full LB2
+	int K, D;
+	float inv_scale;
+	// training-record logging
+	uint8_t *log_rec;         // [log_cap][stride]
+	long long log_cap;
+	int log_stride;
 	int n, stride;
 };
 
@@ -370,6 +384,7 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 		D->region_slots = 0;
 		D->n_fathers = 0;
 		D->n_children = 0;
+		D->n_unsettled = 0;
 		if (top < 0)
 			D->done = 1;
 	}
@@ -818,6 +833,210 @@ __global__ void init_kernel(ExParams P, int ub0, int best, int win_min, int win_
 	}
 }
 
+// ---- learned mode ----------------------------------------------------------
+
+// Features of every father (from the region copy), for the pair selector.
+__global__ void father_features_kernel(ExParams P, BoundParams bp)
+{
+	ExDev *D = P.dev;
+	if (halted(D) || D->n_fathers == 0)
+		return;
+	const int n = P.n, m = bp.m;
+	const uint8_t *tb = bp.t8.blob;
+	const int32_t *pt = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pt);
+	const int32_t *heads = reinterpret_cast<const int32_t *>(tb + bp.t8.off_heads);
+	const int32_t *tails = reinterpret_cast<const int32_t *>(tb + bp.t8.off_tails);
+	const long long nf = D->n_fathers;
+	for (long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x; f < nf;
+	     f += (long long)gridDim.x * blockDim.x) {
+		const int16_t *rec =
+		    reinterpret_cast<const int16_t *>(P.tmp_rec + P.father_ridx[f] * P.stride);
+		int32_t F[WSBB_MAX_MACHINES], G[WSBB_MAX_MACHINES], R[WSBB_MAX_MACHINES];
+		node_times(rec, n, m, pt, F, G);
+		const int l1 = rec[n], l2 = rec[n + 1];
+		for (int k = 0; k < m; ++k) {
+			F[k] = l1 >= 0 ? F[k] : heads[k];
+			R[k] = l2 < n ? G[m - 1 - k] : tails[k];
+		}
+		uint32_t mask[4];
+		free_mask(rec, n, mask);
+		write_features(F, R, mask, n, m, P.inv_scale, P.D, P.feat + f * P.D);
+	}
+}
+
+constexpr int kPartialThreads = 256;
+
+__device__ __forceinline__ bool job_free(const uint32_t (&mask)[4], int job)
+{
+	const uint32_t w01 = (job & 32) ? mask[1] : mask[0];
+	const uint32_t w23 = (job & 32) ? mask[3] : mask[2];
+	return ((((job & 64) ? w23 : w01) >> (job & 31)) & 1u) != 0;
+}
+
+// One warp per father, its children in passes of 32 lanes. Every child of
+// a father is tried on the father's K ranked pairs (so all lanes read the
+// same table entries: broadcasts). A child whose bound over those pairs
+// already reaches max(best, incumbent) keeps that value; the others — and
+// the leaves of simple fathers — go to the full-LB2 list.
+template <int MAXM>
+__global__ void __launch_bounds__(kPartialThreads) partial_kernel(ExParams P, BoundParams bp)
+{
+	extern __shared__ __align__(16) uint8_t smem[];
+	ExDev *D = P.dev;
+	if (halted(D) || D->n_fathers == 0)
+		return;
+	{
+		const uint4 *src = reinterpret_cast<const uint4 *>(bp.t8.blob);
+		uint4 *dst = reinterpret_cast<uint4 *>(smem);
+		for (uint32_t i = threadIdx.x; i < bp.t8.bytes / 16; i += blockDim.x)
+			dst[i] = src[i];
+	}
+	__syncthreads();
+	const int n = P.n, m = bp.m, K = P.K;
+	const uint2 *tj = reinterpret_cast<const uint2 *>(smem);
+	const int32_t *pt = reinterpret_cast<const int32_t *>(smem + bp.t8.off_pt);
+	const int32_t *pairs = reinterpret_cast<const int32_t *>(smem + bp.t8.off_pairs);
+	const int32_t *heads = reinterpret_cast<const int32_t *>(smem + bp.t8.off_heads);
+	const int32_t *tails = reinterpret_cast<const int32_t *>(smem + bp.t8.off_tails);
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+	int32_t *colF = reinterpret_cast<int32_t *>(smem + bp.t8.bytes) + wib * 2 * MAXM * 32;
+	int32_t *colR = colF + MAXM * 32;
+	const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+	const long long nf = D->n_fathers;
+	const int thr = max(D->best, D->ub);
+	for (long long f = warp; f < nf; f += nwarps) {
+		const long long c0 = P.child_off[f];
+		const int nc = int(P.child_off[f + 1] - c0);
+		const long long ridx = P.father_ridx[f];
+		const int16_t *fr = reinterpret_cast<const int16_t *>(P.tmp_rec + ridx * P.stride);
+		const int depth = P.tmp_meta[ridx].depth;
+		if (depth == n - 2) { // leaves: makespans come from the full path
+			const unsigned base = lane == 0 ? (unsigned)atomicAdd(
+			                                      (unsigned long long *)&D->n_unsettled,
+			                                      (unsigned long long)nc)
+			                                : 0u;
+			const unsigned b0 = __shfl_sync(0xffffffffu, base, 0);
+			for (int k = lane; k < nc; k += 32)
+				P.unsettled[b0 + k] = int32_t(c0 + k);
+			continue;
+		}
+		const int l1 = fr[n], l2 = fr[n + 1];
+		const int u = l2 - l1 - 1;
+		// father's raw front / reversed back times (every lane, same values)
+		int32_t Fr[MAXM], Gr[MAXM];
+#pragma unroll
+		for (int k = 0; k < MAXM; ++k)
+			Fr[k] = Gr[k] = 0;
+		for (int j = 0; j <= l1; ++j) {
+			const int job = fr[j];
+			Fr[0] += pt[job];
+#pragma unroll
+			for (int k = 1; k < MAXM; ++k)
+				if (k < m)
+					Fr[k] = max(Fr[k], Fr[k - 1]) + pt[k * n + job];
+		}
+		for (int j = n - 1; j >= l2; --j) {
+			const int job = fr[j];
+			Gr[0] += pt[(m - 1) * n + job];
+#pragma unroll
+			for (int q = 1; q < MAXM; ++q)
+				if (q < m)
+					Gr[q] = max(Gr[q], Gr[q - 1]) + pt[(m - 1 - q) * n + job];
+		}
+		uint32_t fmask[4] = {0, 0, 0, 0};
+		for (int j = l1 + 1; j < l2; ++j)
+			fmask[fr[j] >> 5] |= 1u << (fr[j] & 31);
+		const int16_t *my_pairs = P.fpairs + f * K;
+		for (int pass = 0; pass < nc; pass += 32) {
+			const int k = pass + lane;
+			const bool active = k < nc;
+			const long long c = c0 + (active ? k : 0);
+			const int job = active ? P.child_job[c] : fr[l1 + 1];
+			const bool end_side = k >= u;
+			// the child's front / back: the father's plus the moved job
+			const int fcount = l1 + 1 + (end_side ? 0 : 1);
+			const int bcount = n - l2 + (end_side ? 1 : 0);
+			int32_t prevF = 0, prevG = 0;
+#pragma unroll
+			for (int q = 0; q < MAXM; ++q) {
+				if (q >= m)
+					break;
+				int32_t fv = Fr[q], gv = Gr[q];
+				if (!end_side) {
+					fv = (q == 0 ? Fr[0] : max(prevF, Fr[q])) + pt[q * n + job];
+					prevF = fv;
+				} else {
+					gv = (q == 0 ? Gr[0] : max(prevG, Gr[q])) + pt[(m - 1 - q) * n + job];
+					prevG = gv;
+				}
+				colF[q * 32 + lane] = fcount > 0 ? fv : heads[q];
+				colR[(m - 1 - q) * 32 + lane] = bcount > 0 ? gv : tails[m - 1 - q];
+			}
+			uint32_t mask[4] = {fmask[0], fmask[1], fmask[2], fmask[3]};
+			mask[job >> 5] &= ~(1u << (job & 31));
+			const int32_t tail_off = bcount > 0 ? 0 : -(1 << 30);
+			int32_t part = 0;
+			for (int i = 0; i < K; ++i) {
+				const int pi = my_pairs[i];
+				const int a = pairs[pi] & 0xff, b = pairs[pi] >> 8;
+				int32_t t0 = colF[a * 32 + lane], t1 = colF[b * 32 + lane];
+				const uint2 *e = tj + pi * n;
+				for (int q = 0; q < n; ++q) {
+					const uint2 v = e[q];
+					if (job_free(mask, int(v.x & 0xffu))) {
+						t0 += int32_t(v.x >> 16);
+						t1 = max(t1, t0 + int32_t(v.y >> 16)) + int32_t(v.y & 0xffffu);
+					}
+				}
+				part = max(part, max(t1 + colR[b * 32 + lane], t0 + colR[a * 32 + lane] + tail_off));
+			}
+			const bool settled = active && part >= thr;
+			if (settled)
+				P.child_lb[c] = part;
+			const unsigned open = __ballot_sync(0xffffffffu, active && !settled);
+			const unsigned done = __ballot_sync(0xffffffffu, settled);
+			unsigned base = 0;
+			if (lane == 0) {
+				base = (unsigned)atomicAdd((unsigned long long *)&D->n_unsettled,
+				                           (unsigned long long)__popc(open));
+				if (done)
+					atomicAdd(&D->early, (unsigned long long)__popc(done));
+			}
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if (active && !settled)
+				P.unsettled[base + __popc(open & ((1u << lane) - 1u))] = int32_t(c);
+			__syncwarp();
+		}
+	}
+}
+
+// Training records: a hashed sample of this iteration's bounded children.
+__global__ void log_kernel(ExParams P)
+{
+	ExDev *D = P.dev;
+	if (halted(D) || D->n_fathers == 0 || !P.log_rec)
+		return;
+	const long long total = D->n_children;
+	const unsigned long long it = (unsigned long long)D->iterations;
+	const int S = P.stride;
+	for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < total;
+	     c += (long long)gridDim.x * blockDim.x) {
+		unsigned long long h = (unsigned long long)c * 0x9E3779B97F4A7C15ULL ^ (it << 32);
+		h = (h ^ (h >> 29)) * 0xBF58476D1CE4E5B9ULL;
+		h ^= h >> 32;
+		if (h % (unsigned long long)P.log_stride != 0)
+			continue;
+		const unsigned long long slot = atomicAdd(&D->log_count, 1ull);
+		if (slot >= (unsigned long long)P.log_cap)
+			continue;
+		const uint4 *src = reinterpret_cast<const uint4 *>(P.child_rec + c * S);
+		uint4 *dst = reinterpret_cast<uint4 *>(P.log_rec + slot * S);
+		for (int q = 0; q < S / 16; ++q)
+			dst[q] = src[q];
+	}
+}
+
 // Lays the search buffers out from `base` (null: only sizes them).
 size_t search_layout(uint8_t *base, long long cap, long long region_cap, int window, int n,
                      int S, ExParams &P)
@@ -874,6 +1093,16 @@ struct ExploreState {
 	cudaGraphExec_t graph = nullptr;
 	cudaStream_t graph_stream = nullptr;
 	int graph_iters = 0;
+	// mode of the captured graph: 0 plain, 1 learned, 2 logging
+	int mode = 0;
+	const wsbb_model *model = nullptr;
+	void *learned_mem = nullptr; // features, ranked pairs, unsettled list
+	size_t learned_bytes = 0;
+	int graph_K = 0;
+	void *graph_learned = nullptr;
+	uint8_t *graph_log = nullptr;
+	long long graph_log_cap = 0;
+	int graph_log_stride = 0;
 };
 
 void wsbb_explore_release(wsbb_ctx *ctx)
@@ -884,6 +1113,8 @@ void wsbb_explore_release(wsbb_ctx *ctx)
 		cudaGraphExecDestroy(ctx->ex->graph);
 	if (ctx->ex->mem)
 		cudaFree(ctx->ex->mem);
+	if (ctx->ex->learned_mem)
+		cudaFree(ctx->ex->learned_mem);
 	delete ctx->ex;
 	ctx->ex = nullptr;
 }
@@ -896,7 +1127,9 @@ int ex_fail(wsbb_ctx *ctx, cudaError_t e, const char *what)
 }
 
 // One iteration: a fixed sequence of stream-ordered launches (captured
-// into a graph).
+// into a graph). The learned mode bounds children in two steps (K ranked
+// pairs for all, full LB2 for the ones left open); the logging mode copies
+// a sample of the children out before bounding them.
 cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 {
 	using namespace wsbb;
@@ -909,8 +1142,32 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 	select_write_kernel<<<sel_grid, kSelCtaThreads, 0, s>>>(X.P);
 	father_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	make_children_kernel<<<grid, 256, 0, s>>>(X.P);
-	cudaError_t e = launch_pool_bounds(X.child_bp, X.P.child_rec, X.child_cap, X.P.child_lb, 0,
-	                                   ctx->num_sms, s);
+	cudaError_t e = cudaSuccess;
+	if (X.mode == 1) {
+		father_features_kernel<<<grid, 128, 0, s>>>(X.P, ctx->bp);
+		e = launch_mlp_topk(X.model, X.P.feat, X.window, &X.P.dev->n_fathers, X.P.K, X.P.fpairs,
+		                    nullptr, ctx->num_sms, s);
+		if (e != cudaSuccess)
+			return e;
+		const size_t smem = size_t(ctx->bp.t8.bytes) +
+		                    size_t(kPartialThreads / 32) * 2 * 20 * 32 * 4;
+		auto kern = ctx->bp.m <= 8 ? partial_kernel<8>
+		                           : (ctx->bp.m <= 16 ? partial_kernel<16> : partial_kernel<20>);
+		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+		if (e != cudaSuccess)
+			return e;
+		kern<<<ctx->num_sms, kPartialThreads, smem, s>>>(X.P, ctx->bp);
+		BoundParams gbp = X.child_bp;
+		gbp.count_dev = &X.P.dev->n_unsettled;
+		gbp.gather = X.P.unsettled;
+		e = launch_pool_bounds(gbp, X.P.child_rec, X.child_cap, X.P.child_lb, 0, ctx->num_sms,
+		                       s);
+	} else {
+		if (X.mode == 2)
+			log_kernel<<<grid, 256, 0, s>>>(X.P);
+		e = launch_pool_bounds(X.child_bp, X.P.child_rec, X.child_cap, X.P.child_lb, 0,
+		                       ctx->num_sms, s);
+	}
 	if (e != cudaSuccess)
 		return e;
 	choose_kernel<<<grid, 256, 0, s>>>(X.P);
@@ -945,12 +1202,20 @@ void fill_stats(const wsbb::ExDev &h, const int16_t *best_rec, int n, int status
 	st->seconds = seconds;
 	st->scanned = (int64_t)h.scanned;
 	st->committed = (int64_t)h.committed;
+	st->early = (int64_t)h.early;
 }
 
-}  // namespace
+struct SearchMode {
+	int mode = 0;                 // 0 plain, 1 learned, 2 logging
+	const wsbb_model *model = nullptr;
+	int K = 0;
+	uint8_t *log_rec = nullptr;
+	long long log_cap = 0;
+	int log_stride = 1;
+};
 
-extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *st,
-                            void *stream_v)
+int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, wsbb_stats *st,
+               void *stream_v, long long *logged)
 {
 	using namespace wsbb;
 	if (!ctx || !cfg || !st)
@@ -997,6 +1262,32 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 		X->child_bp.count_dev = &X->P.dev->n_children;
 		ctx->ex = X;
 	}
+	if (M.mode == 1) {
+		int D = 0;
+		wsbb_model_dims(M.model, &D, nullptr, nullptr);
+		const size_t need = size_t(window) * D * 4 + size_t(window) * M.K * 2 + 256 +
+		                    size_t(X->child_cap) * 4 + 256;
+		if (X->learned_bytes < need) {
+			if (X->learned_mem)
+				cudaFree(X->learned_mem);
+			X->learned_mem = nullptr;
+			X->learned_bytes = 0;
+			if (cudaMalloc(&X->learned_mem, need) != cudaSuccess)
+				return wsbb_set_error(ctx, WSBB_ERR_NOMEM, "learned buffers");
+			X->learned_bytes = need;
+		}
+		uint8_t *b = static_cast<uint8_t *>(X->learned_mem);
+		X->P.feat = reinterpret_cast<float *>(b);
+		X->P.fpairs = reinterpret_cast<int16_t *>(b + size_t(window) * D * 4);
+		X->P.unsettled = reinterpret_cast<int32_t *>(
+		    b + ((size_t(window) * D * 4 + size_t(window) * M.K * 2 + 255) & ~size_t(255)));
+		X->P.K = M.K;
+		X->P.D = D;
+		X->P.inv_scale = wsbb_feature_scale(ctx);
+	}
+	X->P.log_rec = M.mode == 2 ? M.log_rec : nullptr;
+	X->P.log_cap = M.mode == 2 ? M.log_cap : 0;
+	X->P.log_stride = M.mode == 2 ? std::max(1, M.log_stride) : 1;
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
 	init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window);
@@ -1006,7 +1297,20 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 
 	const int G = cfg->graph_iters > 0 ? cfg->graph_iters : 16;
 	const bool use_graph = !(cfg->flags & WSBB_EXPLORE_NO_GRAPH);
-	if (use_graph && (!X->graph || X->graph_iters != G || X->graph_stream != s)) {
+	// kernel arguments are captured by value: any change of mode, model, K,
+	// learned buffers or log target needs a new graph
+	const bool stale = X->graph_iters != G || X->graph_stream != s || X->mode != M.mode ||
+	                   X->model != M.model || X->graph_K != X->P.K ||
+	                   X->graph_learned != X->learned_mem || X->graph_log != X->P.log_rec ||
+	                   X->graph_log_cap != X->P.log_cap || X->graph_log_stride != X->P.log_stride;
+	X->mode = M.mode;
+	X->model = M.model;
+	X->graph_K = X->P.K;
+	X->graph_learned = X->learned_mem;
+	X->graph_log = X->P.log_rec;
+	X->graph_log_cap = X->P.log_cap;
+	X->graph_log_stride = X->P.log_stride;
+	if (use_graph && (!X->graph || stale)) {
 		if (X->graph)
 			cudaGraphExecDestroy(X->graph);
 		X->graph = nullptr;
@@ -1069,9 +1373,55 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "incumbent download");
 	fill_stats(h, best_rec.data(), n, status, ms * 1e-3, st);
+	if (logged)
+		*logged = std::min((long long)h.log_count, M.log_cap);
 	if (h.error)
 		return wsbb_set_error(ctx, h.error, "search pool capacity exceeded");
 	return WSBB_OK;
+}
+
+}  // namespace
+
+extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *st,
+                            void *stream)
+{
+	return run_search(ctx, cfg, SearchMode(), st, stream, nullptr);
+}
+
+extern "C" int wsbb_explore_learned(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
+                                    wsbb_model *model, int K, wsbb_stats *st, void *stream)
+{
+	if (!ctx || !model)
+		return WSBB_ERR_ARG;
+	int D = 0, O = 0;
+	wsbb_model_dims(model, &D, &O, nullptr);
+	if (K < 1 || K > 32 || K > ctx->inst.P || ctx->inst.m > 20 ||
+	    D != (2 * ctx->inst.m + ctx->inst.n + 15) / 16 * 16 ||
+	    O != (ctx->inst.P + 7) / 8 * 8)
+		return wsbb_set_error(ctx, WSBB_ERR_ARG, "model does not match the instance or K");
+	SearchMode M;
+	M.mode = 1;
+	M.model = model;
+	M.K = K;
+	return run_search(ctx, cfg, M, st, stream, nullptr);
+}
+
+extern "C" int wsbb_explore_log(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, void *recs_out,
+                                int64_t cap, int stride, int64_t *logged, wsbb_stats *st,
+                                void *stream)
+{
+	if (!ctx || !recs_out || cap <= 0 || stride < 1)
+		return WSBB_ERR_ARG;
+	SearchMode M;
+	M.mode = 2;
+	M.log_rec = static_cast<uint8_t *>(recs_out);
+	M.log_cap = cap;
+	M.log_stride = stride;
+	long long got = 0;
+	const int rc = run_search(ctx, cfg, M, st, stream, &got);
+	if (logged)
+		*logged = got;
+	return rc;
 }
 
 // ---------------------------------------------------------------------------

@@ -66,6 +66,9 @@ struct BoundParams {
 	// When set, the kernels read the record count from device memory and
 	// the host-side count only sizes the grid (graph-captured launches).
 	const long long *count_dev = nullptr;
+	// When set, record i of a launch is record gather[i] of the pool and its
+	// result goes to out[gather[i]].
+	const int32_t *gather = nullptr;
 };
 
 // Kernel launchers (bound_kernels.cu). `mode`: 0 = LB2, 1 = LB1,
@@ -74,6 +77,12 @@ cudaError_t launch_pool_bounds(const BoundParams &bp, const void *recs,
                                int64_t count, int32_t *out, int mode,
                                int num_sms, cudaStream_t stream);
 size_t pool_bounds_smem(const BoundParams &bp, int threads);
+
+// Learned selector inference (learned.cu): top-K pairs of `rows` feature
+// rows (rows_dev, when set, holds the row count on the device).
+cudaError_t launch_mlp_topk(const wsbb_model *md, const float *X, long long rows,
+                            const long long *rows_dev, int K, int16_t *topk, float *logits,
+                            int num_sms, cudaStream_t s);
 
 }  // namespace wsbb
 

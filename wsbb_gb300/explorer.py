@@ -31,7 +31,7 @@ class ExploreStats(C.Structure):
                 ("discarded", C.c_int64), ("iterations", C.c_int64), ("best_cost", C.c_int32),
                 ("status", C.c_int32), ("depth_hist", C.c_uint64 * (MAX_JOBS + 1)),
                 ("best_perm", C.c_int32 * MAX_JOBS), ("seconds", C.c_double),
-                ("scanned", C.c_int64), ("committed", C.c_int64)]
+                ("scanned", C.c_int64), ("committed", C.c_int64), ("early", C.c_int64)]
 
 
 NO_GRAPH = 1
