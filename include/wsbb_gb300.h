@@ -8,8 +8,10 @@
  * (wsbb_last_error() describes the last failure on a context). The caller
  * owns every buffer it passes; a context owns its device tables and its
  * search pools. One context per host thread; calls on a context are
- * stream-ordered on the stream they are given (NULL = the default stream)
- * unless documented as synchronous.
+ * stream-ordered on the stream they are given, unless documented as
+ * synchronous. NULL means the legacy default stream (PyTorch's default
+ * stream): calls that run on the library's own stream instead (the
+ * searches, training) first wait for the work already queued there.
  *
  * Reference interfaces each entry point replaces (vttuan/WSBB paths):
  *   wsbb_ctx_create     bound_abstract::set_instance -> bound_flowshop::init
@@ -126,9 +128,12 @@ int wsbb_lb2_eval_host(wsbb_ctx *ctx, const void *host_recs, int64_t count,
 typedef struct {
 	int32_t ub0;         /* initial incumbent cost (INT32_MAX: none) */
 	int32_t best;        /* choise threshold (the reference default is 99999) */
-	int32_t window;      /* nodes branched per iteration (0: 4096) */
+	int32_t window;      /* largest number of nodes branched per iteration
+	                        (0: 16384); the search widens up to it */
 	int32_t graph_iters; /* iterations per graph launch (0: 16) */
-	int64_t capacity;    /* stack capacity in nodes (0: 2^22) */
+	int64_t capacity;    /* stack capacity in nodes (0: max(2^22, 2 window n^2),
+	                        within half the free device memory); at least
+	                        16 window + 8192 */
 	int64_t max_iters;   /* stop after this many iterations (0: none) */
 	int32_t flags;       /* WSBB_EXPLORE_* */
 	int32_t reserved;
@@ -192,9 +197,10 @@ int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
  * and its pair re-ordering is commented out, :129-130).
  *
  * A 3-layer MLP (D -> 128 -> 128 -> P, ReLU, bf16 operands, fp32
- * accumulation) maps a node's features — effective heads and tails per
- * machine divided by the largest machine load, and the free-job mask;
- * D = round_up(2m + n, 16) — to scores of the P machine pairs. Trained on
+ * accumulation) maps a node's features — effective heads and tails and the
+ * remaining work per machine, divided by the largest machine load, and the
+ * free-job mask; D = round_up(3m + n, 16) — to scores of the P machine
+ * pairs. Trained on
  * the GPU (Adam, softmax cross-entropy against the node's binding pair).
  * In a search it ranks, per father, the K pairs tried first on all of its
  * children; a child whose bound over those K pairs already reaches

@@ -80,7 +80,7 @@ def test_logged_nodes_and_labels_match_oracle(env, oracle):
     recs = torch.empty((cap, ctx.stride), dtype=torch.uint8, device="cuda")
     got, st = Lr.log_nodes(ctx, recs.data_ptr(), cap, stride=3, ub0=ub, max_iters=64)
     assert 0 < got <= cap
-    D = (2 * m + n + 15) // 16 * 16
+    D = (3 * m + n + 15) // 16 * 16
     X = torch.empty((got, D), dtype=torch.float32, device="cuda")
     y = torch.empty(got, dtype=torch.int32, device="cuda")
     Lr.features(ctx, recs.data_ptr(), got, D, X.data_ptr(), y.data_ptr())
@@ -96,12 +96,12 @@ def test_logged_nodes_and_labels_match_oracle(env, oracle):
     # mask features: 1 exactly on the free jobs
     for i in range(0, got, max(1, got // 50)):
         free = set(perms[i][l1[i] + 1:l2[i]].tolist())
-        assert set(np.nonzero(Xn[i, 2 * m:2 * m + n])[0].tolist()) == free
+        assert set(np.nonzero(Xn[i, 3 * m:3 * m + n])[0].tolist()) == free
 
 
 def trained_model(torch, W, Lr, n, m, seeds, per_seed=20000, epochs=4):
     """Log children of plain searches on `seeds`, train a model on them."""
-    D = (2 * m + n + 15) // 16 * 16
+    D = (3 * m + n + 15) // 16 * 16
     Xs, ys = [], []
     for s in seeds:
         p = W.gen_instance(s, n, m)

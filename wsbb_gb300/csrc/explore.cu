@@ -860,7 +860,7 @@ __global__ void father_features_kernel(ExParams P, BoundParams bp)
 		}
 		uint32_t mask[4];
 		free_mask(rec, n, mask);
-		write_features(F, R, mask, n, m, P.inv_scale, P.D, P.feat + f * P.D);
+		write_features(F, R, mask, n, m, pt, P.inv_scale, P.D, P.feat + f * P.D);
 	}
 }
 
@@ -1290,6 +1290,10 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	X->P.log_stride = M.mode == 2 ? std::max(1, M.log_stride) : 1;
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
+	// no caller stream: the training-record buffer may still be in use by
+	// work queued on the legacy default stream
+	if (!stream_v && (e = wait_for_legacy(s)) != cudaSuccess)
+		return ex_fail(ctx, e, "stream ordering");
 	init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window);
 	e = cudaGetLastError();
 	if (e != cudaSuccess)
@@ -1355,8 +1359,8 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 			e = cudaStreamSynchronize(s);
 		if (e != cudaSuccess || h.done || h.error)
 			break;
-		if (launched >= max_iters) {
-			status = 1;
+		if (launched >= max_iters || (M.mode == 2 && (long long)h.log_count >= M.log_cap)) {
+			status = 1; // iteration cap, or the training-record buffer is full
 			break;
 		}
 	}
@@ -1396,7 +1400,7 @@ extern "C" int wsbb_explore_learned(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	int D = 0, O = 0;
 	wsbb_model_dims(model, &D, &O, nullptr);
 	if (K < 1 || K > 32 || K > ctx->inst.P || ctx->inst.m > 20 ||
-	    D != (2 * ctx->inst.m + ctx->inst.n + 15) / 16 * 16 ||
+	    D != (3 * ctx->inst.m + ctx->inst.n + 15) / 16 * 16 ||
 	    O != (ctx->inst.P + 7) / 8 * 8)
 		return wsbb_set_error(ctx, WSBB_ERR_ARG, "model does not match the instance or K");
 	SearchMode M;

@@ -7,8 +7,10 @@
 //                          LB2 itself starts from)
 //             x[m..2m)     effective tails / scale (back times or static
 //                          tails)
-//             x[2m..2m+n)  1 for each job still free
-//             padded with zeros to D = round_up(2m + n, 16); scale = the
+//             x[2m..3m)    remaining work of each machine over the free
+//                          jobs / scale (where the bottleneck is)
+//             x[3m..3m+n)  1 for each job still free
+//             padded with zeros to D = round_up(3m + n, 16); scale = the
 //             largest machine load of the instance
 //   network   D -> 128 -> 128 -> P logits (ReLU), bf16 operands with fp32
 //             accumulation; logits are padded to O = round_up(P, 8)
@@ -69,7 +71,7 @@ __global__ void features_kernel(BoundParams bp, const uint8_t *__restrict__ recs
 		}
 		uint32_t mask[4];
 		free_mask(rec, n, mask);
-		write_features(F, R, mask, n, m, inv_scale, D, X + r * D);
+		write_features(F, R, mask, n, m, pt, inv_scale, D, X + r * D);
 		if (!labels)
 			continue;
 		if (l2 - l1 == 1) {
@@ -182,7 +184,7 @@ void gemm(cudaStream_t s, const float *A, long long sam, long long sak, const fl
 
 // Softmax cross-entropy over the first P of O logits; writes dZ = (softmax -
 // onehot) / B (zero on padding) and adds the batch's loss sum to *loss.
-// Rows with label < 0 contribute nothing. One warp per row.
+// Rows whose label is outside [0, P) contribute nothing. One warp per row.
 __global__ void softmax_xent_kernel(const float *Z, const int32_t *y, int B, int O, int P,
                                     float inv_b, float *dZ, float *loss)
 {
@@ -192,7 +194,7 @@ __global__ void softmax_xent_kernel(const float *Z, const int32_t *y, int B, int
 		return;
 	const float *z = Z + (long long)row * O;
 	float *dz = dZ + (long long)row * O;
-	const int label = y[row];
+	const int label = y[row] < P ? y[row] : -1;
 	float mx = -INFINITY;
 	for (int o = lane; o < P; o += 32)
 		mx = fmaxf(mx, z[o]);
@@ -550,7 +552,7 @@ extern "C" int wsbb_model_create(int n, int m, uint64_t seed, wsbb_model **out)
 	md->n = n;
 	md->m = m;
 	md->P = m * (m - 1) / 2;
-	md->D = (2 * m + n + 15) / 16 * 16;
+	md->D = (3 * m + n + 15) / 16 * 16;
 	md->O = (md->P + 7) / 8 * 8;
 	const Offsets of = offsets_of(md->D, md->O);
 	md->nparams = of.total;
@@ -670,11 +672,13 @@ extern "C" int wsbb_features(wsbb_ctx *ctx, const void *recs, int64_t count, flo
 {
 	if (!ctx || count < 0 || (count > 0 && (!recs || !X)))
 		return WSBB_ERR_ARG;
-	if (D < 2 * ctx->inst.m + ctx->inst.n)
-		return wsbb_set_error(ctx, WSBB_ERR_ARG, "feature width below 2m + n");
+	if (D < 3 * ctx->inst.m + ctx->inst.n)
+		return wsbb_set_error(ctx, WSBB_ERR_ARG, "feature width below 3m + n");
 	if (count == 0)
 		return WSBB_OK;
-	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+	// no caller stream: the legacy default stream, ordered with the
+	// caller's default-stream work on `recs`, `X` and `labels`
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	const int grid = int(std::min<int64_t>((count + 127) / 128, ctx->num_sms * 16));
 	wsbb::features_kernel<<<grid, 128, 0, s>>>(ctx->bp, static_cast<const uint8_t *>(recs),
 	                                           count, inv_scale, D, X, labels);
@@ -702,8 +706,11 @@ extern "C" int wsbb_model_grads(wsbb_model *md, const float *X, const int32_t *y
 	if (!md || !X || !y || B <= 0)
 		return WSBB_ERR_ARG;
 	cudaStream_t s = md->stream;
+	cudaError_t e = wsbb::wait_for_legacy(s); // X, y may come from default-stream work
+	if (e != cudaSuccess)
+		return model_fail(md, WSBB_ERR_CUDA, cudaGetErrorString(e));
 	cudaMemsetAsync(md->d_loss, 0, sizeof(float), s);
-	cudaError_t e = forward_backward(md, X, y, B, s);
+	e = forward_backward(md, X, y, B, s);
 	if (e == cudaSuccess && grad_host)
 		e = cudaMemcpyAsync(grad_host, md->grad, sizeof(float) * md->nparams,
 		                    cudaMemcpyDeviceToHost, s);
@@ -725,7 +732,9 @@ extern "C" int wsbb_model_train(wsbb_model *md, const float *X, const int32_t *y
 	float *xb = nullptr;
 	int32_t *yb = nullptr;
 	long long *idx = nullptr;
-	cudaError_t e = cudaMalloc(&xb, sizeof(float) * size_t(batch) * D);
+	cudaError_t e = wsbb::wait_for_legacy(s); // X, y may come from default-stream work
+	if (e == cudaSuccess)
+		e = cudaMalloc(&xb, sizeof(float) * size_t(batch) * D);
 	if (e == cudaSuccess)
 		e = cudaMalloc(&yb, sizeof(int32_t) * batch);
 	if (e == cudaSuccess)
@@ -818,7 +827,7 @@ extern "C" int wsbb_model_topk(wsbb_model *md, const float *X, int64_t rows, int
 	int dev = 0, sms = 0;
 	cudaGetDevice(&dev);
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : md->stream;
+	cudaStream_t s = static_cast<cudaStream_t>(stream); // NULL: the legacy default stream
 	cudaError_t e = wsbb::launch_mlp_topk(md, X, rows, nullptr, K, topk, logits, sms, s);
 	return e == cudaSuccess ? WSBB_OK : model_fail(md, WSBB_ERR_CUDA, cudaGetErrorString(e));
 }

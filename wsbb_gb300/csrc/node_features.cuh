@@ -43,19 +43,26 @@ __device__ __forceinline__ void free_mask(const int16_t *rec, int n, uint32_t (&
 }
 
 // Features of a node with effective heads He[k] and tails Te[k] (what LB2
-// starts from) and free-job mask `mask`: He / scale, Te / scale rounded to
-// bf16, the mask as 0/1, zero padding up to D.
+// starts from) and free-job mask `mask`: He / scale, Te / scale and the
+// remaining work of each machine over the free jobs / scale, each rounded
+// to bf16, then the mask as 0/1, zero padding up to D.
 __device__ __forceinline__ void write_features(const int32_t *He, const int32_t *Te,
                                                const uint32_t (&mask)[4], int n, int m,
-                                               float inv_scale, int D, float *x)
+                                               const int32_t *pt, float inv_scale, int D,
+                                               float *x)
 {
 	for (int k = 0; k < m; ++k) {
+		int32_t work = 0;
+		for (int j = 0; j < n; ++j)
+			if ((mask[j >> 5] >> (j & 31)) & 1u)
+				work += pt[k * n + j];
 		x[k] = __bfloat162float(__float2bfloat16_rn(float(He[k]) * inv_scale));
 		x[m + k] = __bfloat162float(__float2bfloat16_rn(float(Te[k]) * inv_scale));
+		x[2 * m + k] = __bfloat162float(__float2bfloat16_rn(float(work) * inv_scale));
 	}
 	for (int j = 0; j < n; ++j)
-		x[2 * m + j] = (mask[j >> 5] >> (j & 31)) & 1u ? 1.f : 0.f;
-	for (int d = 2 * m + n; d < D; ++d)
+		x[3 * m + j] = (mask[j >> 5] >> (j & 31)) & 1u ? 1.f : 0.f;
+	for (int d = 3 * m + n; d < D; ++d)
 		x[d] = 0.f;
 }
 

@@ -84,6 +84,25 @@ cudaError_t launch_mlp_topk(const wsbb_model *md, const float *X, long long rows
                             const long long *rows_dev, int K, int16_t *topk, float *logits,
                             int num_sms, cudaStream_t s);
 
+// Orders the library's own stream `s` after the work already queued on the
+// legacy default stream, where a caller given no stream (PyTorch's default
+// stream among them) writes the buffers it passes in. A non-blocking
+// stream does not wait on the legacy stream by itself.
+inline cudaError_t wait_for_legacy(cudaStream_t s)
+{
+	if (s == nullptr || s == cudaStreamLegacy)
+		return cudaSuccess;
+	cudaEvent_t ev;
+	cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+	if (e != cudaSuccess)
+		return e;
+	e = cudaEventRecord(ev, cudaStreamLegacy);
+	if (e == cudaSuccess)
+		e = cudaStreamWaitEvent(s, ev, 0);
+	cudaEventDestroy(ev);
+	return e;
+}
+
 }  // namespace wsbb
 
 struct wsbb_ctx {

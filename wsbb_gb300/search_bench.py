@@ -1,10 +1,15 @@
 """Search benchmark: time-to-proof and bounded nodes/s of the GPU search.
 
     python -m wsbb_gb300.search_bench --n 50 --m 10 --seeds 0 1 2 3 4
+    python -m wsbb_gb300.search_bench --n 50 --m 10 --best ub0 \
+        --model wsbb_gb300/models/selector_n50_m10.npz --K 4 8
 
 Each run proves the optimum of one seeded instance (values uniform in
-[1, 99]) from the NEH incumbent, exactly as the reference CPU search would
-explore it (same tree), and prints one JSON object per run plus a summary.
+[1, 99]) from the NEH incumbent, exploring exactly the tree the reference
+CPU search explores with the same `best` (side-choice threshold), and
+prints one JSON object per run plus a summary. With --model, every
+instance is also searched with the learned K-pair test (same tree, checked)
+and the speed-up over the plain search at the same `best` is reported.
 """
 from __future__ import annotations
 
@@ -15,9 +20,16 @@ import sys
 from .bound import Context, gen_instance, neh
 from .explorer import explore
 
+TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost", "coverage")
+
 
 def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: str = "default",
-        device: int = 0, verbose: bool = True) -> dict:
+        device: int = 0, verbose: bool = True, model_path: str = "", Ks=(8,)) -> dict:
+    model = None
+    if model_path:
+        from .learned import Model
+        model = Model(n, m)
+        model.load(model_path)
     runs = []
     for s in seeds:
         p = gen_instance(s, n, m)
@@ -33,16 +45,37 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
                "scanned": r["scanned"], "committed": r["committed"],
                "seconds": r["seconds"],
                "bounded_per_s": r["bounded"] / max(r["seconds"], 1e-12)}
+        if model is not None:
+            from .learned import explore_learned
+            row["learned"] = {}
+            for K in Ks:
+                q = explore_learned(ctx, model, K, ub0=ub0, best=best, window=window,
+                                    max_iters=max_iters)
+                same = all(q[k] == r[k] for k in TREE_KEYS)
+                row["learned"][str(K)] = {
+                    "seconds": q["seconds"], "early": q["early"],
+                    "early_share": q["early"] / max(1, q["evaluated"]),
+                    "same_tree": same, "speedup": r["seconds"] / max(q["seconds"], 1e-12),
+                    "bounded_per_s": q["bounded"] / max(q["seconds"], 1e-12)}
         runs.append(row)
         ctx.close()
         if verbose:
             print(json.dumps(row), flush=True)
     tot_b = sum(r["bounded"] for r in runs)
     tot_s = sum(r["seconds"] for r in runs)
-    return {"runs": runs, "bounded": tot_b, "seconds": tot_s,
-            "bounded_per_s": tot_b / max(tot_s, 1e-12),
-            "evaluated": sum(r["evaluated"] for r in runs),
-            "all_proved": all(r["proved"] for r in runs)}
+    out = {"runs": runs, "bounded": tot_b, "seconds": tot_s,
+           "bounded_per_s": tot_b / max(tot_s, 1e-12),
+           "evaluated": sum(r["evaluated"] for r in runs),
+           "all_proved": all(r["proved"] for r in runs)}
+    if model is not None:
+        out["learned"] = {}
+        for K in Ks:
+            ls = sum(r["learned"][str(K)]["seconds"] for r in runs)
+            out["learned"][str(K)] = {
+                "seconds": ls, "bounded_per_s": tot_b / max(ls, 1e-12),
+                "speedup_vs_plain": tot_s / max(ls, 1e-12),
+                "same_tree": all(r["learned"][str(K)]["same_tree"] for r in runs)}
+    return out
 
 
 def main(argv=None) -> None:
@@ -53,8 +86,10 @@ def main(argv=None) -> None:
     ap.add_argument("--window", type=int, default=0)
     ap.add_argument("--max-iters", type=int, default=0)
     ap.add_argument("--best", default="default", choices=["default", "ub0"])
+    ap.add_argument("--model", default="")
+    ap.add_argument("--K", type=int, nargs="+", default=[8])
     a = ap.parse_args(argv)
-    out = run(a.n, a.m, a.seeds, a.window, a.max_iters, a.best)
+    out = run(a.n, a.m, a.seeds, a.window, a.max_iters, a.best, model_path=a.model, Ks=a.K)
     summary = {k: v for k, v in out.items() if k != "runs"}
     print(json.dumps({"summary": summary}), flush=True)
 
