@@ -106,6 +106,22 @@ int wsbb_lb1_eval(wsbb_ctx *ctx, const void *recs, int64_t count,
 int wsbb_makespan_eval(wsbb_ctx *ctx, const void *recs, int64_t count,
                        int32_t *out, void *stream);
 
+/* Branch and bound a batch of fathers, asynchronous on `stream`: both sides
+ * of every father (decompose_beginend::operator(),
+ * src/decompose_beginend.cpp:91-107, bounding each child with
+ * bornes_calculer, src/bound_flowshop.cpp:929-951). Father f's children
+ * are child_off[f] .. child_off[f+1]-1 (device int64, count + 1 entries):
+ * its u BEGIN children (the job at free position l1+1+k moved to l1+1),
+ * then its u END children (moved to l2-1); a father with two free jobs has
+ * two leaf children (both orders; their makespans). child_lb gets each
+ * child's LB2 (bit-exact to bounding the child record with wsbb_lb2_eval),
+ * child_job the job it moved. The children share one pass over each
+ * pair's Johnson order of the father's free jobs (max-plus prefix and
+ * suffix products), so no child record is materialised. */
+int wsbb_decompose_lb2(wsbb_ctx *ctx, const void *fathers, int64_t count,
+                       const int64_t *child_off, int32_t *child_lb,
+                       int16_t *child_job, void *stream);
+
 /* Synchronous host-buffer form of wsbb_lb2_eval: copies the records to the
  * device, bounds them and copies the bounds back before returning. */
 int wsbb_lb2_eval_host(wsbb_ctx *ctx, const void *host_recs, int64_t count,
@@ -123,7 +139,10 @@ int wsbb_lb2_eval_host(wsbb_ctx *ctx, const void *host_recs, int64_t count,
  * the sequential search's exactly. The search state stays on the device;
  * iterations are replayed from a CUDA graph.
  */
-#define WSBB_EXPLORE_NO_GRAPH 1 /* launch iterations one by one */
+#define WSBB_EXPLORE_NO_GRAPH 1  /* launch iterations one by one */
+#define WSBB_EXPLORE_CHILD_LB2 2 /* bound each child record on its own (the
+                                    per-node LB2 kernel) instead of each
+                                    father's children together; same bounds */
 
 typedef struct {
 	int32_t ub0;         /* initial incumbent cost (INT32_MAX: none) */

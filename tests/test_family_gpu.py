@@ -1,0 +1,110 @@
+"""Family bounds (wsbb_decompose_lb2): every child's LB2 from its father,
+bit-exact to the oracle's bound of the child record, and the search with
+family bounds exploring the same tree as with per-child bounds."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import wsbb_gb300 as W
+    return torch, W
+
+
+def random_fathers(rng, n, count):
+    """Father records with every cursor shape: the root, empty fronts or
+    backs, two free jobs (leaf children) up to n free."""
+    perms = np.array([rng.permutation(n) for _ in range(count)], dtype=np.int32)
+    l1 = np.empty(count, np.int32)
+    l2 = np.empty(count, np.int32)
+    for i in range(count):
+        kind = i % 6
+        if kind == 0:                      # root
+            a, u = -1, n
+        elif kind == 1:                    # nothing at the back
+            u = int(rng.integers(2, n + 1))
+            a = n - 1 - u
+        elif kind == 2:                    # nothing at the front
+            a, u = -1, int(rng.integers(2, n + 1))
+        elif kind == 3:                    # two free jobs: leaves
+            a = int(rng.integers(-1, n - 2))
+            u = 2
+        else:
+            a = int(rng.integers(-1, n - 2))
+            u = int(rng.integers(2, n - a))
+        l1[i], l2[i] = a, a + 1 + u
+    return perms, l1, l2
+
+
+@pytest.mark.parametrize("n,m,count", [(3, 2, 12), (8, 5, 60), (20, 20, 90), (50, 20, 60),
+                                       (50, 10, 60), (100, 20, 24), (128, 16, 12),
+                                       (33, 7, 40)])
+def test_family_bounds_match_oracle(env, oracle, n, m, count):
+    torch, W = env
+    rng = np.random.default_rng(n * 100 + m)
+    p = W.gen_instance(n + m, n, m)
+    ctx = W.Context(p)
+    perms, l1, l2 = random_fathers(rng, n, count)
+    fathers = W.pack_records(perms, l1, l2)
+    kids, off = W.expand_children(fathers, n)
+    d_f = torch.from_numpy(fathers).cuda()
+    d_off = torch.from_numpy(off).cuda()
+    lb = torch.full((len(kids),), -7, dtype=torch.int32, device="cuda")
+    job = torch.full((len(kids),), -7, dtype=torch.int16, device="cuda")
+    ctx.decompose_lb2(d_f.data_ptr(), count, d_off.data_ptr(), lb.data_ptr(), job.data_ptr())
+    torch.cuda.synchronize()
+    kp, k1, k2 = W.unpack_records(kids, n)
+    want = oracle.Bound(p).eval_batch(kp, k1, k2)
+    np.testing.assert_array_equal(lb.cpu().numpy(), want)
+    # the moved job: the one a child fixes that its father left free
+    moved = []
+    for f in range(count):
+        for c in range(off[f], off[f + 1]):
+            a, b = int(k1[c]), int(k2[c])
+            fa = int(l1[f])
+            moved.append(int(kp[c][fa + 1]) if a > fa else int(kp[c][b]))
+    np.testing.assert_array_equal(job.cpu().numpy(), np.array(moved, dtype=np.int16))
+
+
+def test_family_bounds_equal_per_child_kernel(env):
+    """Same bounds as the pool kernel on the expanded children, at a pool
+    size where every CTA takes many fathers."""
+    torch, W = env
+    n, m, count = 50, 20, 3000
+    rng = np.random.default_rng(7)
+    p = W.gen_instance(3, n, m)
+    ctx = W.Context(p)
+    perms, l1, l2 = random_fathers(rng, n, count)
+    fathers = W.pack_records(perms, l1, l2)
+    kids, off = W.expand_children(fathers, n)
+    d_f = torch.from_numpy(fathers).cuda()
+    d_k = torch.from_numpy(kids).cuda()
+    d_off = torch.from_numpy(off).cuda()
+    lb = torch.empty(len(kids), dtype=torch.int32, device="cuda")
+    job = torch.empty(len(kids), dtype=torch.int16, device="cuda")
+    ref = torch.empty(len(kids), dtype=torch.int32, device="cuda")
+    ctx.decompose_lb2(d_f.data_ptr(), count, d_off.data_ptr(), lb.data_ptr(), job.data_ptr())
+    ctx.lb2_eval(d_k.data_ptr(), len(kids), ref.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(lb, ref)
+
+
+@pytest.mark.parametrize("n,m,seed,best", [(20, 20, 1, "ub0"), (50, 10, 0, "default"),
+                                           (12, 5, 3, "default")])
+def test_search_same_tree_family_and_per_child(env, n, m, seed, best):
+    torch, W = env
+    from wsbb_gb300.explorer import explore
+    p = W.gen_instance(seed, n, m)
+    ub, _ = W.neh(p)
+    b = ub if best == "ub0" else 99999
+    ctx = W.Context(p)
+    fam = explore(ctx, ub0=ub, best=b, max_iters=120)
+    per = explore(ctx, ub0=ub, best=b, max_iters=120, child_lb2=True)
+    for k in ("branched", "pruned", "leaves", "improved", "bounded", "evaluated", "discarded",
+              "iterations", "best_cost", "status", "coverage", "scanned", "committed"):
+        assert fam[k] == per[k], k

@@ -97,3 +97,30 @@ def test_record_layout(W):
     perms, l1, l2 = W.unpack_records(rec, 20)
     assert (l1[0], l2[0]) == (3, 17)
     assert rec.nbytes == 48
+
+
+def test_child_order_partitions_the_permutations(W):
+    """Expanding from the root, keeping one side of every father at random
+    (the choice the search makes), reaches every permutation exactly once
+    as a leaf; each child fixes one job its father left free."""
+    n = 6
+    rng = np.random.default_rng(0)
+    root = W.pack_records(np.arange(n)[None, :], [-1], [n])
+    leaves, stack = [], [root[0]]
+    while stack:
+        r = stack.pop()
+        kids, off = W.expand_children(r[None, :], n)
+        u = int(r[n + 1]) - int(r[n]) - 1
+        assert len(kids) == (2 if u == 2 else 2 * u)
+        if u == 2:
+            leaves += [tuple(k[:n]) for k in kids]
+            assert all(k[n + 1] - k[n] == 1 and k[n + 2] == n for k in kids)
+            continue
+        free = set(r[int(r[n]) + 1:int(r[n + 1])].tolist())
+        side = int(rng.integers(0, 2))
+        for k in kids[side * u:(side + 1) * u]:
+            assert sorted(k[:n].tolist()) == list(range(n))
+            assert set(k[int(k[n]) + 1:int(k[n + 1])].tolist()) < free
+            assert int(k[n + 2]) == int(r[n + 2]) + 1
+            stack.append(k)
+    assert len(leaves) == 720 and len(set(leaves)) == 720

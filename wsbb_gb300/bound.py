@@ -44,6 +44,42 @@ def unpack_records(rec: np.ndarray, n: int):
             rec[:, n + 1].astype(np.int32))
 
 
+def expand_children(rec: np.ndarray, n: int):
+    """Children of father records in the library's order (host restatement
+    of the begin-end branching, src/decompose_beginend.cpp:26-89 with
+    bb_problem_calculator::create_raw_problem3 / limites_set,
+    src/bb_problem_calculator.cpp:25-48): per father, the u BEGIN children
+    (free position l1+1+k moved to l1+1) then the u END children (moved to
+    l2-1); a father with two free jobs has the two orders of them as leaves.
+    Returns (child records, child_off) with child_off[f] the first child of
+    father f."""
+    rec = np.asarray(rec)
+    out, off = [], [0]
+    for r in rec:
+        l1, l2, depth = int(r[n]), int(r[n + 1]), int(r[n + 2])
+        u = l2 - l1 - 1
+        kids = []
+        if u == 2:
+            for k in range(2):
+                c = r.copy()
+                c[l1 + 1], c[l1 + 1 + k] = r[l1 + 1 + k], r[l1 + 1]
+                c[n], c[n + 1], c[n + 2] = l1 + 2, l2, n
+                kids.append(c)
+        else:
+            for side in (0, 1):
+                for k in range(u):
+                    c = r.copy()
+                    ind = l1 + 1 + k
+                    slot = l2 - 1 if side else l1 + 1
+                    c[ind], c[slot] = r[slot], r[ind]
+                    c[n], c[n + 1] = (l1, l2 - 1) if side else (l1 + 1, l2)
+                    c[n + 2] = depth + 1
+                    kids.append(c)
+        out.extend(kids)
+        off.append(off[-1] + len(kids))
+    return np.array(out, dtype=np.int16).reshape(-1, rec.shape[1]), np.array(off, np.int64)
+
+
 def gen_instance(seed: int, n: int, m: int) -> np.ndarray:
     """Seeded instance: p[k, j] uniform in [1, 99] (SplitMix64, machine-major)."""
     p = np.empty(m * n, dtype=np.int32)
@@ -116,6 +152,13 @@ class Context:
     def makespan_eval(self, recs_ptr: int, count: int, out_ptr: int, stream: int = 0) -> None:
         check(self.h, lib().wsbb_makespan_eval(self.h, recs_ptr, count, out_ptr,
                                                stream or None))
+
+    def decompose_lb2(self, fathers_ptr: int, count: int, child_off_ptr: int, lb_ptr: int,
+                      job_ptr: int, stream: int = 0) -> None:
+        """Bounds of every child of `count` father records (device), in the
+        order of expand_children; child_off (int64, count + 1) on the device."""
+        check(self.h, lib().wsbb_decompose_lb2(self.h, fathers_ptr, count, child_off_ptr, lb_ptr,
+                                               job_ptr, stream or None))
 
     # host-buffer entry point (synchronous)
     def lb2_eval_host(self, recs: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:

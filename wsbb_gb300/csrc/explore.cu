@@ -1103,6 +1103,10 @@ struct ExploreState {
 	uint8_t *graph_log = nullptr;
 	long long graph_log_cap = 0;
 	int graph_log_stride = 0;
+	// children bounded one record at a time (pool LB2 kernel) instead of
+	// per father (family bounds)
+	bool child_lb2 = false;
+	bool graph_child_lb2 = false;
 };
 
 void wsbb_explore_release(wsbb_ctx *ctx)
@@ -1165,8 +1169,20 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 	} else {
 		if (X.mode == 2)
 			log_kernel<<<grid, 256, 0, s>>>(X.P);
-		e = launch_pool_bounds(X.child_bp, X.P.child_rec, X.child_cap, X.P.child_lb, 0,
-		                       ctx->num_sms, s);
+		if (X.child_lb2) {
+			e = launch_pool_bounds(X.child_bp, X.P.child_rec, X.child_cap, X.P.child_lb, 0,
+			                       ctx->num_sms, s);
+		} else {
+			FamilyArgs fa;
+			fa.fathers = X.P.tmp_rec;
+			fa.ridx = X.P.father_ridx;
+			fa.count_dev = &X.P.dev->n_fathers;
+			fa.child_off = X.P.child_off;
+			fa.child_lb = X.P.child_lb;
+			fa.child_job = X.P.child_job;
+			fa.stride = X.P.stride;
+			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms, s);
+		}
 	}
 	if (e != cudaSuccess)
 		return e;
@@ -1303,7 +1319,9 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	const bool use_graph = !(cfg->flags & WSBB_EXPLORE_NO_GRAPH);
 	// kernel arguments are captured by value: any change of mode, model, K,
 	// learned buffers or log target needs a new graph
+	X->child_lb2 = (cfg->flags & WSBB_EXPLORE_CHILD_LB2) != 0;
 	const bool stale = X->graph_iters != G || X->graph_stream != s || X->mode != M.mode ||
+	                   X->graph_child_lb2 != X->child_lb2 ||
 	                   X->model != M.model || X->graph_K != X->P.K ||
 	                   X->graph_learned != X->learned_mem || X->graph_log != X->P.log_rec ||
 	                   X->graph_log_cap != X->P.log_cap || X->graph_log_stride != X->P.log_stride;
@@ -1314,6 +1332,7 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	X->graph_log = X->P.log_rec;
 	X->graph_log_cap = X->P.log_cap;
 	X->graph_log_stride = X->P.log_stride;
+	X->graph_child_lb2 = X->child_lb2;
 	if (use_graph && (!X->graph || stale)) {
 		if (X->graph)
 			cudaGraphExecDestroy(X->graph);
@@ -1503,6 +1522,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	X.window = window;
 	X.child_bp = ctx->bp;
 	X.child_bp.count_dev = &X.P.dev->n_children;
+	X.child_lb2 = (cfg->flags & WSBB_EXPLORE_CHILD_LB2) != 0;
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
 	const auto t0 = std::chrono::steady_clock::now();

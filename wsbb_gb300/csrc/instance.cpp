@@ -224,6 +224,14 @@ HostTables pack_tables(const Instance &I, std::string &err)
 	H.img8 = pack_image(I, 8, H.t8);
 	if (I.n <= 32)
 		H.img16 = pack_image(I, 16, H.t16);
+	// position-major copy of the 8-byte Johnson entries
+	const size_t entries = size_t(I.P) * I.n;
+	H.imgT.resize(entries * 8);
+	const uint64_t *src = reinterpret_cast<const uint64_t *>(H.img8.data());
+	uint64_t *dst = reinterpret_cast<uint64_t *>(H.imgT.data());
+	for (int i = 0; i < I.P; ++i)
+		for (int q = 0; q < I.n; ++q)
+			dst[size_t(q) * I.P + i] = src[size_t(i) * I.n + q];
 	if (H.t8.bytes > 200 * 1024)
 		err = "bound tables exceed the shared-memory budget (n * m too large)";
 	return H;

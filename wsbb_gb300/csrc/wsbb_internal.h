@@ -46,14 +46,18 @@ struct TableView {
 };
 
 struct DeviceTables {
-	void *mem = nullptr; // both images in one allocation
+	void *mem = nullptr; // all images in one allocation
 	size_t bytes = 0;
 	TableView t8, t16;   // t16.blob is null when n > 32
+	// The 8-byte Johnson entries position-major, johnsonT[q * P + i] = entry
+	// q of pair i, so that threads walking consecutive pairs read
+	// consecutive entries (family bounds).
+	const uint2 *johnsonT = nullptr;
 };
 
-// Host images of the two tables; offsets are relative to each image.
+// Host images of the tables; offsets are relative to each image.
 struct HostTables {
-	std::vector<uint8_t> img8, img16;
+	std::vector<uint8_t> img8, img16, imgT;
 	TableView t8, t16;
 };
 HostTables pack_tables(const Instance &inst, std::string &err);
@@ -77,6 +81,23 @@ cudaError_t launch_pool_bounds(const BoundParams &bp, const void *recs,
                                int64_t count, int32_t *out, int mode,
                                int num_sms, cudaStream_t stream);
 size_t pool_bounds_smem(const BoundParams &bp, int threads);
+
+// Family bounds (family.cu): LB2 of every child of each father, in the
+// search's child order (the father's u BEGIN children, then its u END
+// children; two leaves when it has two free jobs).
+struct FamilyArgs {
+	const uint8_t *fathers = nullptr;    // father records
+	const long long *ridx = nullptr;     // father f is record ridx[f] (null: f)
+	long long count = 0;                 // fathers, when count_dev is null
+	const long long *count_dev = nullptr;
+	const long long *child_off = nullptr; // [count + 1] first child of each father
+	int32_t *child_lb = nullptr;
+	int16_t *child_job = nullptr;        // the job each child moves
+	int stride = 0;                      // record stride in bytes
+};
+cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, const FamilyArgs &A,
+                              long long max_fathers, int num_sms, cudaStream_t s);
+size_t family_smem(const BoundParams &bp);
 
 // Learned selector inference (learned.cu): top-K pairs of `rows` feature
 // rows (rows_dev, when set, holds the row count on the device).

@@ -35,6 +35,7 @@ class ExploreStats(C.Structure):
 
 
 NO_GRAPH = 1
+CHILD_LB2 = 2  # bound every child record on its own instead of per father (same bounds)
 
 
 def coverage(hist, n: int) -> int:
@@ -44,11 +45,15 @@ def coverage(hist, n: int) -> int:
 
 def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int = 0,
             graph_iters: int = 0, capacity: int = 0, max_iters: int = 0, graph: bool = True,
-            stream: int = 0) -> dict:
+            stream: int = 0, child_lb2: bool = False) -> dict:
+    """The exact GPU search. `child_lb2` bounds each child record on its own
+    with the per-node LB2 kernel (the reference GPU kernel's form) instead of
+    each father's children together; bounds and tree are the same."""
     L = lib()
     L.wsbb_explore.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    flags = (0 if graph else NO_GRAPH) | (CHILD_LB2 if child_lb2 else 0)
     cfg = ExploreCfg(INT32_MAX if ub0 is None else int(ub0), int(best), int(window),
-                     int(graph_iters), int(capacity), int(max_iters), 0 if graph else NO_GRAPH, 0)
+                     int(graph_iters), int(capacity), int(max_iters), flags, 0)
     st = ExploreStats()
     rc = L.wsbb_explore(ctx.h, C.byref(cfg), C.byref(st), stream or None)
     if rc != 0:

@@ -24,7 +24,10 @@ TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost",
 
 
 def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: str = "default",
-        device: int = 0, verbose: bool = True, model_path: str = "", Ks=(8,)) -> dict:
+        device: int = 0, verbose: bool = True, model_path: str = "", Ks=(8,),
+        per_child: bool = False) -> dict:
+    """`per_child` also runs the search with every child bounded on its own
+    (the per-node LB2 kernel) and reports its time and tree check."""
     model = None
     if model_path:
         from .learned import Model
@@ -45,6 +48,13 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
                "scanned": r["scanned"], "committed": r["committed"],
                "seconds": r["seconds"],
                "bounded_per_s": r["bounded"] / max(r["seconds"], 1e-12)}
+        if per_child:
+            q = explore(ctx, ub0=ub0, best=best, window=window, max_iters=max_iters,
+                        child_lb2=True)
+            row["per_child"] = {"seconds": q["seconds"],
+                                "same_tree": all(q[k] == r[k] for k in TREE_KEYS),
+                                "bounded_per_s": q["bounded"] / max(q["seconds"], 1e-12),
+                                "family_speedup": q["seconds"] / max(r["seconds"], 1e-12)}
         if model is not None:
             from .learned import explore_learned
             row["learned"] = {}
@@ -67,6 +77,11 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
            "bounded_per_s": tot_b / max(tot_s, 1e-12),
            "evaluated": sum(r["evaluated"] for r in runs),
            "all_proved": all(r["proved"] for r in runs)}
+    if per_child:
+        ps = sum(r["per_child"]["seconds"] for r in runs)
+        out["per_child"] = {"seconds": ps, "bounded_per_s": tot_b / max(ps, 1e-12),
+                            "family_speedup": ps / max(tot_s, 1e-12),
+                            "same_tree": all(r["per_child"]["same_tree"] for r in runs)}
     if model is not None:
         out["learned"] = {}
         for K in Ks:
@@ -88,8 +103,11 @@ def main(argv=None) -> None:
     ap.add_argument("--best", default="default", choices=["default", "ub0"])
     ap.add_argument("--model", default="")
     ap.add_argument("--K", type=int, nargs="+", default=[8])
+    ap.add_argument("--per-child", action="store_true",
+                    help="also search with per-child LB2 (the per-node kernel)")
     a = ap.parse_args(argv)
-    out = run(a.n, a.m, a.seeds, a.window, a.max_iters, a.best, model_path=a.model, Ks=a.K)
+    out = run(a.n, a.m, a.seeds, a.window, a.max_iters, a.best, model_path=a.model, Ks=a.K,
+              per_child=a.per_child)
     summary = {k: v for k, v in out.items() if k != "runs"}
     print(json.dumps({"summary": summary}), flush=True)
 
