@@ -1,20 +1,34 @@
-"""Bounded nodes per second of the GB300 LB2 pool path (and its CPU arms).
+"""Bounded nodes per second of the exact GB300 flowshop search, with the
+per-child, learned and CPU arms on the same tree.
 
-Workload (one step = one LB2 launch over one pool): permutation flowshop,
-n = 20 jobs, m = 20 machines (190 machine pairs), processing times uniform
-in [1, 99] from seeds 0-9; one pool of 2^20 partial permutations per
-instance (int16 job ids + begin/end cursors, 48-byte records; seeded
-uniform-random front/back splits with a 2 % share of leaves). Steps rotate
-over the 10 instances, so the 10 pools (503 MB) exceed the 129 MB L2
-between uses of the same pool.
+Workload (one step = one search): permutation flowshop n = 50 jobs, m = 20
+machines (190 machine pairs), processing times uniform in [1, 99] from seed
+0; begin-end branching from the NEH incumbent with side-choice threshold
+best = NEH (the learned-selector configuration), 400 batched iterations of
+at most 16384 fathers each. Every step explores the same tree prefix (its
+counters are checked against the first step's). The search state grows to
+gigabytes over a step, far beyond the 129 MB L2; L2 is also flushed between
+steps.
 
-  value  device-resident pools: records bounded / second (CUDA events on
-         the launching stream, max over ranks)
-  e2e    the same through the synchronous host-buffer C-ABI call
-         (wsbb_lb2_eval_host) from pinned memory: upload, bound, download
-  cpu_baseline / --impl reference: the CPU port of the reference bound
-         (oracle/, bit-exact to the reference's compiled bound_flowshop)
-         on the host cores
+  value  bounded nodes (child LB2 evaluations of the tree) per second of
+         the search with family bounds (every child of a father bounded
+         from the father's shared max-plus pair passes), the search state
+         resident in HBM; CUDA events on the launching stream, max over
+         ranks
+  arms   the same tree searched with per-child LB2 (the reference GPU
+         kernel's form), with the learned K-pair test ahead of per-child
+         LB2, and with the learned test ahead of family bounds
+  e2e    the same metric through the C-ABI from host memory: every step
+         creates the context from the host instance (table upload), runs
+         the search (state reads, stats and incumbent to the host) and
+         destroys it
+  roofline  the dominant kernel (family bounds) on a father pool through
+         wsbb_decompose_lb2, against the INT32 add/max issue peak measured
+         in this run
+  cpu_baseline / --impl reference: the CPU port of the reference explorer
+         (oracle/, its semantics and counters) on the host cores
+Sections: the LB2 pool kernel (n=20 m=20 pools of 2^20 records) and the
+time-to-proof of the n=50 m=10 instances (seeds 0-4).
 """
 from __future__ import annotations
 
@@ -32,34 +46,29 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_JOBS, N_MACH, POOL, SEEDS, LEAF_SHARE = 20, 20, 1 << 20, 10, 0.02
-METRIC = "bounded nodes/sec (LB2 pool, n=20 m=20)"
-UNIT = "nodes/s"
+METRIC = ("bounded nodes/sec & time-to-proof (learned+batched vs plain GPU LB2 vs CPU), "
+          "same tree")
+UNIT = "bounded nodes/s"
+S_N, S_M, S_ITERS = 50, 20, 400
+MODEL = os.path.join(ROOT, "wsbb_gb300", "models", f"selector_n{S_N}_m{S_M}.npz")
+TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost", "coverage")
+# kernels per search iteration (family bounds): commit, doom, select x3,
+# father scan, region copy, family bounds, choose, kept scan, emit, finish
+KERNELS_PER_ITER = 12
+
+POOL_N, POOL_M, POOL, POOL_SEEDS, LEAF_SHARE = 20, 20, 1 << 20, 10, 0.02
+PROOF_N, PROOF_M, PROOF_SEEDS = 50, 10, (0, 1, 2, 3, 4)
 
 
-def workload_config(extra: dict | None = None) -> dict:
-    cfg = {"workload": "LB2 pool bounds: n=20 jobs, m=20 machines (190 pairs), seeds 0-9, "
-                       "one 2^20-record pool per instance, rotated",
-           "n": N_JOBS, "m": N_MACH, "pool_records": POOL, "instances": SEEDS,
-           "record_bytes": 48, "leaf_share": LEAF_SHARE,
-           "l2": "inputs larger than L2 (10 pools x 50.3 MB rotate)"}
+def workload_config(seed: int, extra: dict | None = None) -> dict:
+    cfg = {"workload": f"exact begin-end DFS, n={S_N} jobs m={S_M} machines (190 pairs), "
+                       f"seed {seed}, NEH incumbent, best=NEH, {S_ITERS} batched iterations "
+                       "(window <= 16384 fathers) per step",
+           "n": S_N, "m": S_M, "seed": seed, "iterations_per_step": S_ITERS,
+           "l2": "search state >> L2 (GBs), L2 flushed between steps"}
     if extra:
         cfg.update(extra)
     return cfg
-
-
-def alg_ops(recs: np.ndarray, n: int, m: int) -> int:
-    """Algorithmic int32 operations of LB2 over a pool: 4 per (pair,
-    unscheduled job) step, 3 per pair epilogue, 2 per (fixed job, machine)
-    of the front / back times; a leaf is 2 * n * m (its makespan)."""
-    P = m * (m - 1) // 2
-    l1 = recs[:, n].astype(np.int64)
-    l2 = recs[:, n + 1].astype(np.int64)
-    leaf = (l2 - l1) == 1
-    u = l2 - l1 - 1
-    fixed = n - u
-    ops = np.where(leaf, 2 * n * m, 4 * P * u + 3 * P + 2 * fixed * m)
-    return int(ops.sum())
 
 
 class ClockSampler:
@@ -107,70 +116,48 @@ class ClockSampler:
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def cpu_port_rate(nthreads: int, count: int, seed: int = 0) -> tuple[float, dict]:
-    """The CPU port of the reference bound (oracle/) on `count` records."""
+# ------------------------------------------------------------ CPU (oracle port)
+
+def cpu_search_rate(seed: int, threads: int, seconds: float, n: int = S_N, m: int = S_M,
+                    best_is_ub: bool = True) -> dict:
+    """The oracle's sequential explorer (the reference CPU explorer's
+    semantics and counters) on the headline instance, capped by takes so
+    that one run lasts about `seconds`. With threads > 1, that many
+    independent explorer runs of the same sample in parallel (ctypes drops
+    the GIL): the throughput of the host cores, as independent reference
+    peers would give it."""
+    from concurrent.futures import ThreadPoolExecutor
+
     from oracle import oracle as O
-    p = O.gen_instance(seed, N_JOBS, N_MACH)
-    perms, l1, l2 = O.random_pool(1000 + seed, N_JOBS, count, LEAF_SHARE)
-    b = O.Bound(p)
-    b.eval_batch(perms[:256], l1[:256], l2[:256], nthreads=nthreads)
-    t0 = time.perf_counter()
-    b.eval_batch(perms, l1, l2, nthreads=nthreads)
-    dt = time.perf_counter() - t0
-    return count / dt, {"kind": "port", "cores": nthreads,
-                        "sample": f"{count} records of the n=20 m=20 seed-{seed} pool, "
-                                  f"{nthreads} host threads, {dt:.2f} s"}
-
-
-SEARCH_N, SEARCH_M, SEARCH_SEEDS = 50, 10, (0, 1, 2, 3, 4)
-
-
-def cpu_search_rate(seconds: float = 10.0) -> dict:
-    """The oracle's sequential search (the reference CPU explorer's
-    semantics, single-threaded like one reference peer) on the first search
-    instance, capped by node count: bounded nodes per second."""
-    from oracle import oracle as O
-    p = O.gen_instance(SEARCH_SEEDS[0], SEARCH_N, SEARCH_M)
+    p = O.gen_instance(seed, n, m)
     ub, _ = O.neh(p)
-    b = O.Bound(p)
-    cap = 2000
+    best = ub if best_is_ub else 99999
+    cap = 500
     while True:
         t0 = time.perf_counter()
-        rc, st, _ = b.explore(ub0=ub, node_cap=cap)
+        O.Bound(p).explore(ub0=ub, best=best, node_cap=cap)
         dt = time.perf_counter() - t0
-        if dt > seconds / 4 or rc == 0:
+        if dt > seconds / 8:
             break
-        cap *= 4
-    return {"value": st["bounded"] / dt, "unit": "bounded nodes/s", "cores": 1, "kind": "port",
-            "sample": f"first {cap} takes of the n={SEARCH_N} m={SEARCH_M} seed-"
-                      f"{SEARCH_SEEDS[0]} search, {dt:.1f} s"}
+        cap *= 2
+    cap = max(cap, int(cap * seconds / max(dt, 1e-3)))
 
+    def one(_):
+        rc, st, _ = O.Bound(p).explore(ub0=ub, best=best, node_cap=cap)
+        return st["bounded"]
 
-def search_section(cpu: bool) -> dict:
-    """Time-to-proof of the exact GPU search on the persistent-explorer
-    instances (n=50, m=10, seeds 0-4, NEH incumbent)."""
-    from wsbb_gb300 import search_bench
-    out = search_bench.run(SEARCH_N, SEARCH_M, SEARCH_SEEDS, verbose=False)
-    sec = {"workload": f"exact DFS time-to-proof, n={SEARCH_N} m={SEARCH_M}, seeds "
-                       f"{list(SEARCH_SEEDS)}, NEH initial incumbent, best=99999; tree "
-                       "identical to the reference CPU search",
-           "all_proved": out["all_proved"], "time_to_proof_s": out["seconds"],
-           "bounded_nodes": out["bounded"], "bounded_nodes_per_s": out["bounded_per_s"],
-           "evaluated_bounds": out["evaluated"],
-           "per_instance": [{k: r[k] for k in ("seed", "optimum", "branched", "pruned",
-                                               "leaves", "bounded", "seconds")}
-                            for r in out["runs"]]}
-    if cpu:
-        c = cpu_search_rate()
-        sec["cpu_baseline"] = c
-        sec["cpu_est_time_to_proof_s"] = out["bounded"] / c["value"]
-    return sec
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        total = sum(ex.map(one, range(threads)))
+    dt = time.perf_counter() - t0
+    return {"value": total / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {cap} takes of the n={n} m={m} seed-{seed} search "
+                      f"(best={'NEH' if best_is_ub else 99999}), "
+                      f"{threads} independent run(s) in parallel, {dt:.1f} s"}
 
 
 def run_reference(args) -> None:
@@ -178,34 +165,160 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    count = 1 << 17
     for _ in range(args.warmup):
-        cpu_port_rate(cores, 1 << 12)
-    rates = []
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        r, info = cpu_port_rate(cores, count, seed=k % SEEDS)
-        rates.append(r)
+        cpu_search_rate(0, 1, 0.2)
+    rates, t0 = [], time.perf_counter()
+    for _ in range(args.steps):
+        rates.append(cpu_search_rate(0, cores, 3.0))
     wall = time.perf_counter() - t0
-    value = args.steps * count / sum(count / r for r in rates)
+    value = statistics.mean(r["value"] for r in rates)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": workload_config({"sample_records_per_step": count}),
+            "config": workload_config(0, {"parallelism": "host threads"}),
             "cpu_baseline": {"value": value, "unit": UNIT, "kind": "port", "cores": cores,
-                             "sample": f"{count} records per step of the n=20 m=20 pools "
-                                       f"(seeds rotate), {cores} host threads; the reference's "
-                                       "compiled bound cannot run on this host (its tree is "
-                                       "absent), the port is bit-exact to it"},
+                             "sample": rates[-1]["sample"] + "; the reference's compiled "
+                             "explorer cannot run on this host (its source tree is absent), "
+                             "the port reproduces its node counts exactly"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args) -> None:
+# ------------------------------------------------------------------- GPU arms
+
+def family_alg_ops(recs: np.ndarray, n: int, m: int) -> int:
+    """Algorithmic int32 operations of family bounds over a father pool:
+    per (pair, free job) 7 in the forward and 12 in the backward max-plus
+    pass; per (child, pair) 9 (two ends of the walk, two back terms, the
+    max); 2 per (fixed job, machine) for the father's front and back and 4
+    per (free job, machine) for the children's. Two-free-job fathers: their
+    two leaves' makespans (3 per machine each)."""
+    P = m * (m - 1) // 2
+    l1 = recs[:, n].astype(np.int64)
+    l2 = recs[:, n + 1].astype(np.int64)
+    u = l2 - l1 - 1
+    fixed = n - u
+    ops = np.where(u == 2, 2 * fixed * m + 6 * m,
+                   19 * P * u + 9 * P * 2 * u + 2 * fixed * m + 4 * u * m)
+    return int(ops.sum())
+
+
+def father_pool(seed: int, n: int, count: int) -> np.ndarray:
+    """Fathers with u free jobs uniform in [3, n], front / back split uniform."""
+    import wsbb_gb300 as W
+    rng = np.random.default_rng(seed)
+    perms = np.argsort(rng.random((count, n)), axis=1).astype(np.int32)
+    u = rng.integers(3, n + 1, count)
+    f = (rng.random(count) * (n - u + 1)).astype(np.int64)
+    l1 = (f - 1).astype(np.int32)
+    l2 = (f + u).astype(np.int32)
+    return W.pack_records(perms, l1, l2)
+
+
+def roofline_family(ctx, dev, stream, sptr, peak) -> dict:
     import torch
     import wsbb_gb300 as W
+    count = 1 << 15
+    recs = father_pool(11, S_N, count)
+    u = recs[:, S_N + 1].astype(np.int64) - recs[:, S_N].astype(np.int64) - 1
+    nkids = np.where(u == 2, 2, 2 * u)
+    off = np.concatenate([[0], np.cumsum(nkids)]).astype(np.int64)
+    d_f = torch.from_numpy(recs).to(dev)
+    d_off = torch.from_numpy(off).to(dev)
+    lb = torch.empty(int(off[-1]), dtype=torch.int32, device=dev)
+    job = torch.empty(int(off[-1]), dtype=torch.int16, device=dev)
+    for _ in range(3):
+        ctx.decompose_lb2(d_f.data_ptr(), count, d_off.data_ptr(), lb.data_ptr(), job.data_ptr(),
+                          sptr)
+    launches = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(launches):
+        ctx.decompose_lb2(d_f.data_ptr(), count, d_off.data_ptr(), lb.data_ptr(), job.data_ptr(),
+                          sptr)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) * 1e-3 / launches
+    ops = family_alg_ops(recs, S_N, S_M)
+    achieved = ops / t
+    bytes_ = recs.nbytes + off.nbytes + int(off[-1]) * 6
+    return {"bound": "int32", "achieved": achieved / 1e12,
+            "peak": peak / 1e12 if peak else None, "unit": "Tops/s",
+            "frac": achieved / peak if peak else None, "traffic": None,
+            "kernel": "family_kernel (wsbb_decompose_lb2)",
+            "workload": f"{count} fathers n={S_N} m={S_M}, u uniform in [3, {S_N}]",
+            "launch_ms": t * 1e3, "ops_per_launch": ops,
+            "peak_source": "measured in this run: add+max chains on every SM "
+                           "(wsbb_probe_maxplus_peak)",
+            "hbm_achieved_gbs": bytes_ / t / 1e9,
+            "traffic_note": "DRAM traffic per launch is in the committed ncu summary: "
+                            "the kernel's tables stay in L2"}
+
+
+def lb2_pool_section(dev, stream, sptr, peak, launches: int) -> dict:
+    """The per-record LB2 kernel on pools of 2^20 records (n=20 m=20,
+    seeds 0-9, rotated so that the 503 MB of pools exceed L2)."""
+    import torch
+    import wsbb_gb300 as W
+    ctxs, pools, ops = [], [], []
+    P = POOL_M * (POOL_M - 1) // 2
+    for s in range(POOL_SEEDS):
+        ctxs.append(W.Context(W.gen_instance(s, POOL_N, POOL_M), device=dev.index))
+        recs = W.gen_pool(1000 + s, POOL_N, POOL, LEAF_SHARE)
+        l1 = recs[:, POOL_N].astype(np.int64)
+        l2 = recs[:, POOL_N + 1].astype(np.int64)
+        u = l2 - l1 - 1
+        ops.append(int(np.where(u == 0, 2 * POOL_N * POOL_M,
+                                4 * P * u + 3 * P + 2 * (POOL_N - u) * POOL_M).sum()))
+        pools.append(torch.from_numpy(recs).to(dev))
+    out = torch.empty(POOL, dtype=torch.int32, device=dev)
+    for k in range(3):
+        ctxs[k].lb2_eval(pools[k].data_ptr(), POOL, out.data_ptr(), sptr)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(launches)]
+    torch.cuda.synchronize(dev)
+    for k in range(launches):
+        ev[k][0].record(stream)
+        ctxs[k % POOL_SEEDS].lb2_eval(pools[k % POOL_SEEDS].data_ptr(), POOL, out.data_ptr(),
+                                      sptr)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    t = statistics.mean(ms) * 1e-3
+    op = statistics.mean(ops[k % POOL_SEEDS] for k in range(launches))
+    return {"workload": "LB2 of pools of 2^20 records, n=20 m=20 (190 pairs), seeds 0-9 "
+                        "rotated (pools exceed L2)",
+            "records_per_s": launches * POOL / (sum(ms) * 1e-3), "launches": launches,
+            "roofline": {"bound": "int32", "achieved": op / t / 1e12,
+                         "peak": peak / 1e12 if peak else None, "unit": "Tops/s",
+                         "frac": op / t / peak if peak else None,
+                         "kernel": "lb2_fast_kernel"},
+            "hbm_gbs": POOL * 52 / t / 1e9}
+
+
+def proof_section() -> dict:
+    from wsbb_gb300 import search_bench
+    out = search_bench.run(PROOF_N, PROOF_M, PROOF_SEEDS, verbose=False)
+    return {"workload": f"exact DFS to a proven optimum, n={PROOF_N} m={PROOF_M}, seeds "
+                        f"{list(PROOF_SEEDS)}, NEH incumbent, best=99999 (the reference default)",
+            "all_proved": out["all_proved"], "time_to_proof_s": out["seconds"],
+            "bounded_nodes": out["bounded"], "bounded_nodes_per_s": out["bounded_per_s"],
+            "per_instance": [{k: r[k] for k in ("seed", "optimum", "branched", "pruned",
+                                                "leaves", "bounded", "seconds")}
+                             for r in out["runs"]]}
+
+
+def run_gpu(args) -> None:
+    import ctypes as C
+
+    import torch
+
+    import wsbb_gb300 as W
+    from wsbb_gb300.explorer import explore
+    from wsbb_gb300.learned import Model, explore_learned
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -218,119 +331,135 @@ def run_gpu(args) -> None:
         if world > 1:
             torch.distributed.barrier()
 
-    ctxs, d_pools, ops = [], [], []
-    for s in range(SEEDS):
-        p = W.gen_instance(s, N_JOBS, N_MACH)
-        ctxs.append(W.Context(p, device=local))
-        recs = W.gen_pool(1000 + s + 100 * rank, N_JOBS, POOL, LEAF_SHARE)
-        ops.append(alg_ops(recs, N_JOBS, N_MACH))
-        d_pools.append(torch.from_numpy(recs).to(dev))
-    out = torch.empty(POOL, dtype=torch.int32, device=dev)
+    def reduce_max(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def reduce_sum(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        return float(t.item())
+
+    # replicas: rank r searches instance seed r (weak scaling)
+    seed = rank
+    p = W.gen_instance(seed, S_N, S_M)
+    ub0, _ = W.neh(p)
+    ctx = W.Context(p, device=local)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
-    def step(k):
-        ctxs[k % SEEDS].lb2_eval(d_pools[k % SEEDS].data_ptr(), POOL, out.data_ptr(), sptr)
+    def step():
+        return explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr)
 
-    for k in range(args.warmup):
-        step(k)
-    torch.cuda.synchronize(dev)
-
+    ref = None
+    for _ in range(args.warmup):
+        r = step()
+        ref = ref or r
     peak = None
-    import ctypes as C
     pk = C.c_double(0)
     if W.lib().wsbb_probe_maxplus_peak(local, C.byref(pk)) == 0:
         peak = pk.value
 
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
+    same = True
+    bounded = 0
     barrier()
     torch.cuda.synchronize(dev)
     with ClockSampler(local) as clk:
         t_wall = time.perf_counter()
         for k in range(args.steps):
+            flush.zero_()
             ev[k][0].record(stream)
-            step(k)
+            r = step()
             ev[k][1].record(stream)
+            bounded += r["bounded"]
+            same &= all(r[key] == ref[key] for key in TREE_KEYS)
         torch.cuda.synchronize(dev)
         t_wall = time.perf_counter() - t_wall
     barrier()
-    per_launch_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(per_launch_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * POOL / (total_ms * 1e-3)
-    mean_launch_s = statistics.mean(per_launch_ms) * 1e-3
-    ops_per_launch = statistics.mean(ops[k % SEEDS] for k in range(args.steps))
-    bytes_per_launch = POOL * (48 + 4)
+    total_ms = reduce_max(sum(a.elapsed_time(b) for a, b in ev))
+    all_bounded = reduce_sum(float(bounded))
+    value = all_bounded / (total_ms * 1e-3)
+    launches = args.steps * (ref["iterations"] * KERNELS_PER_ITER + 1)
 
-    # end to end through the host-buffer C-ABI call, pinned host memory
-    h_pools = [torch.from_numpy(W.gen_pool(1000 + s + 100 * rank, N_JOBS, POOL, LEAF_SHARE))
-               .pin_memory() for s in range(2)]
-    h_out = torch.empty(POOL, dtype=torch.int32).pin_memory()
-    lib = W.lib()
-    for k in range(2):
-        lib.wsbb_lb2_eval_host(ctxs[k].h, h_pools[k].data_ptr(), POOL, h_out.data_ptr())
-    e2e_steps = max(3, min(args.steps, 30))
+    # end to end through the C-ABI from host memory
+    L = W.lib()
+    h_p = np.ascontiguousarray(p, dtype=np.int32)
+    from wsbb_gb300.explorer import ExploreCfg, ExploreStats
+    cfg = ExploreCfg(ub0, ub0, 0, 0, 0, S_ITERS, 0, 0)
+    e2e_steps = max(2, min(args.steps, 5))
+    h2d = d2h = 0
+    e2e_bounded = 0
     barrier()
     t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        rc = lib.wsbb_lb2_eval_host(ctxs[k % 2].h, h_pools[k % 2].data_ptr(), POOL,
-                                    h_out.data_ptr())
+    for _ in range(e2e_steps):
+        h = C.c_void_p()
+        rc = L.wsbb_ctx_create(h_p.ctypes.data, S_N, S_M, local, C.byref(h))
         if rc != 0:
-            raise RuntimeError(f"wsbb_lb2_eval_host failed: {rc}")
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * e2e_steps * POOL / e2e_s
+            raise RuntimeError(f"wsbb_ctx_create failed: {rc}")
+        st = ExploreStats()
+        rc = L.wsbb_explore(h, C.byref(cfg), C.byref(st), None)
+        if rc != 0:
+            raise RuntimeError(f"wsbb_explore failed: {rc}")
+        h2d = int(L.wsbb_ctx_device_bytes(h)) + C.sizeof(cfg)
+        d2h = int(st.d2h_bytes) + C.sizeof(st)
+        e2e_bounded += st.bounded
+        L.wsbb_ctx_destroy(h)
+    e2e_s = reduce_max(time.perf_counter() - t0)
+    e2e_value = reduce_sum(float(e2e_bounded)) / e2e_s
 
-    search = None
-    if not args.no_search:
-        search = search_section(cpu=(rank == 0 and world == 1))
+    arms = sections = cpu = roof = None
     if rank == 0:
-        cpu = None
+        def arm(r, base_s):
+            return {"seconds": r["seconds"], "bounded_per_s": r["bounded"] / r["seconds"],
+                    "same_tree": all(r[k] == ref[k] for k in TREE_KEYS),
+                    "speedup_vs_per_child_lb2": base_s / r["seconds"]}
+        fam = step()
+        per = explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr, child_lb2=True)
+        arms = {"per_child_lb2": arm(per, per["seconds"]), "family_lb2": arm(fam, per["seconds"])}
+        if os.path.exists(MODEL):
+            model = Model(S_N, S_M)
+            model.load(MODEL)
+            for K, pc in ((16, True), (4, False)):
+                q = explore_learned(ctx, model, K, ub0=ub0, best=ub0, max_iters=S_ITERS,
+                                    stream=sptr, child_lb2=pc)
+                a = arm(q, per["seconds"])
+                a["early_share"] = q["early"] / max(1, q["evaluated"])
+                a["settled_fathers_share"] = q["settled_fathers"] / max(1, q["branched"])
+                arms[f"learned_k{K}_{'per_child' if pc else 'family'}_lb2"] = a
+        roof = roofline_family(ctx, dev, stream, sptr, peak)
+        sections = {"lb2_pool": lb2_pool_section(dev, stream, sptr, peak, 40)}
+        if not args.no_proof:
+            sections["time_to_proof"] = proof_section()
         if world == 1:
             cores = os.cpu_count() or 1
-            rate, info = cpu_port_rate(cores, 1 << 19)
-            cpu = {"value": rate, "unit": UNIT, **info}
-        achieved_ops = ops_per_launch / mean_launch_s
-        hbm_peak, hbm_src = 6800.0, "fallback (no MEASURED_PEAKS.json)"
-        try:
-            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-                hbm_peak = float(json.load(f)["hbm_gbs"])
-                hbm_src = "MEASURED_PEAKS.json hbm_gbs (measured)"
-        except Exception:
-            pass
+            cpu = cpu_search_rate(0, cores, 8.0)
+            cpu["single_thread"] = cpu_search_rate(0, 1, 4.0)["value"]
+            if sections.get("time_to_proof"):
+                tp = sections["time_to_proof"]
+                c10 = cpu_search_rate(PROOF_SEEDS[0], 1, 4.0, PROOF_N, PROOF_M, False)
+                tp["cpu_baseline_1_core"] = c10
+                tp["cpu_est_time_to_proof_s_1_core"] = tp["bounded_nodes"] / c10["value"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": workload_config({"parallelism": f"replicas{world}"}),
-            "roofline": {"bound": "int32", "achieved": achieved_ops / 1e12,
-                         "peak": (peak / 1e12) if peak else None, "unit": "Tops/s",
-                         "frac": (achieved_ops / peak) if peak else None, "traffic": None,
-                         "kernel": "lb2_pool_kernel",
-                         "peak_source": "measured in this run: add+max chains on every SM "
-                                        "(wsbb_probe_maxplus_peak)",
-                         "ops_per_launch": ops_per_launch},
-            "roofline_hbm": {"bound": "hbm", "achieved": bytes_per_launch / mean_launch_s / 1e9,
-                             "peak": hbm_peak, "unit": "GB/s",
-                             "frac": bytes_per_launch / mean_launch_s / 1e9 / hbm_peak,
-                             "peak_source": hbm_src,
-                             "bytes_per_launch": bytes_per_launch},
-            "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": POOL * 48, "d2h_bytes_per_step": POOL * 4,
-                    "steps": e2e_steps},
-            "clocks": clk.summary(),
-            "gpu_launches": args.steps,
-            "wall_s_timed": t_wall,
-            "search": search,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic",
+            "config": workload_config(seed, {"parallelism": f"replicas{world}",
+                                             "bounded_per_step": ref["bounded"],
+                                             "same_tree_every_step": same}),
+            "roofline": roof, "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": e2e_steps},
+            "clocks": clk.summary(), "gpu_launches": launches, "wall_s_timed": t_wall,
+            "arms": arms, "sections": sections,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -340,11 +469,11 @@ def run_gpu(args) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="wsbb", choices=["wsbb", "reference"])
-    ap.add_argument("--no-search", action="store_true",
-                    help="skip the time-to-proof section (search workload)")
+    ap.add_argument("--no-proof", action="store_true",
+                    help="skip the time-to-proof section (n=50 m=10, seeds 0-4)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -77,6 +77,8 @@ int wsbb_ctx_create(const int32_t *p_mxn, int n, int m, int device,
                     wsbb_ctx **out);
 void wsbb_ctx_destroy(wsbb_ctx *ctx);
 const char *wsbb_last_error(const wsbb_ctx *ctx);
+/* Bytes of bound tables wsbb_ctx_create copied host -> device. */
+size_t wsbb_ctx_device_bytes(const wsbb_ctx *ctx);
 
 /* Copies of the host-side precompute (for inspection and tests): pair
  * machines (P each), lags and Johnson orders (P x n), static heads and
@@ -175,6 +177,10 @@ typedef struct {
 	int64_t scanned;    /* stack entries scanned to select fathers */
 	int64_t committed;  /* stack entries committed */
 	int64_t early;      /* children settled by the learned K-pair test */
+	int64_t settled_fathers; /* fathers whose children the K-pair test settled
+	                            all (family bounds) */
+	int64_t d2h_bytes;  /* bytes the search copied device -> host (its state
+	                       between graph launches, the incumbent) */
 } wsbb_stats;
 
 int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,

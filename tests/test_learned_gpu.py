@@ -148,11 +148,13 @@ def test_learned_search_keeps_the_tree(env):
         ub, _ = W.neh(p)
         plain = E.explore(ctx, ub0=ub, best=ub, window=2048)
         for K in (4, 8):
-            got = Lr.explore_learned(ctx, model, K, ub0=ub, best=ub, window=2048)
-            for k in ("branched", "pruned", "leaves", "improved", "bounded", "best_cost",
-                      "coverage", "status"):
-                assert got[k] == plain[k], (seed, K, k)
-            assert got["early"] > 0
+            for per_child in (False, True):
+                got = Lr.explore_learned(ctx, model, K, ub0=ub, best=ub, window=2048,
+                                         child_lb2=per_child)
+                for k in ("branched", "pruned", "leaves", "improved", "bounded", "best_cost",
+                          "coverage", "status"):
+                    assert got[k] == plain[k], (seed, K, per_child, k)
+                assert got["early"] > 0
     # and against the oracle's sequential search with the same best
     from oracle import oracle as O
     p = W.gen_instance(1, 20, 10)

@@ -60,6 +60,9 @@ def _declare_optional(L: C.CDLL) -> None:
     vp = C.c_void_p
     if hasattr(L, "wsbb_explore"):
         L.wsbb_explore.argtypes = [vp, vp, vp, vp]
+    if hasattr(L, "wsbb_ctx_device_bytes"):
+        L.wsbb_ctx_device_bytes.argtypes = [vp]
+        L.wsbb_ctx_device_bytes.restype = C.c_size_t
     if hasattr(L, "wsbb_decompose_lb2"):
         L.wsbb_decompose_lb2.argtypes = [vp, vp, C.c_int64, vp, vp, vp, vp]
 

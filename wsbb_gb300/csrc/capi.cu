@@ -127,6 +127,11 @@ extern "C" void wsbb_ctx_destroy(wsbb_ctx *ctx)
 	delete ctx;
 }
 
+extern "C" size_t wsbb_ctx_device_bytes(const wsbb_ctx *ctx)
+{
+	return ctx ? ctx->tables.bytes : 0;
+}
+
 extern "C" const char *wsbb_last_error(const wsbb_ctx *ctx)
 {
 	return ctx ? ctx->last_error.c_str() : "null context";

@@ -102,6 +102,7 @@ struct ExDev {
 	unsigned long long branched, pruned, leaves, improved, bounded;
 	unsigned long long evaluated, discarded, scanned, committed;
 	unsigned long long early;      // children settled by the learned K-pair test
+	unsigned long long settled_fathers; // fathers whose children it settled all
 	long long n_unsettled;         // children left for full LB2 this iteration
 	unsigned long long log_count;  // training records written
 	unsigned long long hist[WSBB_MAX_JOBS + 1];
@@ -573,8 +574,9 @@ __global__ void __launch_bounds__(kSelThreads) father_scan_kernel(ExParams P)
 	}
 }
 
-// Copy the region aside and write every father's child records.
-__global__ void make_children_kernel(ExParams P)
+// Copy the region aside and, when a later step reads them (per-child
+// bounds, the learned test, logging), write every father's child records.
+__global__ void make_children_kernel(ExParams P, int write_children)
 {
 	ExDev *D = P.dev;
 	if (D->done || D->error || D->n_fathers == 0)
@@ -592,6 +594,8 @@ __global__ void make_children_kernel(ExParams P)
 	}
 	for (long long r = gtid; r < rlen; r += gsz)
 		P.tmp_meta[r] = P.meta[top - r];
+	if (!write_children)
+		return;
 	// children: one thread per child record
 	const long long total = D->n_children;
 	for (long long c = gtid; c < total; c += gsz) {
@@ -767,7 +771,10 @@ __global__ void emit_kernel(ExParams P)
 		}
 		const Meta fm = P.tmp_meta[r];
 		const bool simple = fm.depth == n - 2;
-		const long long c0 = P.child_off[f] + P.father_side[f];
+		const int side_off = P.father_side[f];
+		const long long c0 = P.child_off[f] + side_off;
+		const int16_t *fr16 = reinterpret_cast<const int16_t *>(P.tmp_rec + r * S);
+		const int fl1 = fr16[n], fl2 = fr16[n + 1];
 		const int kept_all = simple ? 2 : int(P.child_off[f + 1] - P.child_off[f]) / 2;
 		const int open = P.father_kept[f];
 		for (int k = lane; k < kept_all; k += 32) {
@@ -776,10 +783,19 @@ __global__ void emit_kernel(ExParams P)
 			if (rank >= open)
 				continue; // pruned at birth: counted with the marker
 			const long long slot = hi_slot - 1 - rank;
-			const uint4 *cs = reinterpret_cast<const uint4 *>(P.child_rec + ck * S);
+			// the child record: the father's with the moved job swapped into
+			// its slot and the new cursors (make_children_kernel's rule)
 			uint4 *dst = reinterpret_cast<uint4 *>(P.rec + slot * S);
 			for (int c = 0; c < S / 16; ++c)
-				dst[c] = cs[c];
+				dst[c] = src[c];
+			int16_t *d16 = reinterpret_cast<int16_t *>(dst);
+			const int indice = fl1 + 1 + k;
+			const int to = (simple || side_off == 0) ? fl1 + 1 : fl2 - 1;
+			d16[indice] = fr16[to];
+			d16[to] = fr16[indice];
+			d16[n] = int16_t(simple ? fl1 + 2 : (side_off == 0 ? fl1 + 1 : fl1));
+			d16[n + 1] = int16_t((simple || side_off == 0) ? fl2 : fl2 - 1);
+			d16[n + 2] = int16_t(simple ? n : fm.depth + 1);
 			Meta cm;
 			cm.lb = P.child_lb[ck];
 			cm.depth = uint8_t(simple ? n : fm.depth + 1);
@@ -1145,7 +1161,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 	select_plan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	select_write_kernel<<<sel_grid, kSelCtaThreads, 0, s>>>(X.P);
 	father_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
-	make_children_kernel<<<grid, 256, 0, s>>>(X.P);
+	make_children_kernel<<<grid, 256, 0, s>>>(X.P, X.mode == 2 || X.child_lb2);
 	cudaError_t e = cudaSuccess;
 	if (X.mode == 1) {
 		father_features_kernel<<<grid, 128, 0, s>>>(X.P, ctx->bp);
@@ -1153,19 +1169,42 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 		                    nullptr, ctx->num_sms, s);
 		if (e != cudaSuccess)
 			return e;
-		const size_t smem = size_t(ctx->bp.t8.bytes) +
-		                    size_t(kPartialThreads / 32) * 2 * 20 * 32 * 4;
-		auto kern = ctx->bp.m <= 8 ? partial_kernel<8>
-		                           : (ctx->bp.m <= 16 ? partial_kernel<16> : partial_kernel<20>);
-		e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-		if (e != cudaSuccess)
-			return e;
-		kern<<<ctx->num_sms, kPartialThreads, smem, s>>>(X.P, ctx->bp);
-		BoundParams gbp = X.child_bp;
-		gbp.count_dev = &X.P.dev->n_unsettled;
-		gbp.gather = X.P.unsettled;
-		e = launch_pool_bounds(gbp, X.P.child_rec, X.child_cap, X.P.child_lb, 0, ctx->num_sms,
-		                       s);
+		if (X.child_lb2) {
+			// per child: the K ranked pairs, then full LB2 for the children
+			// they do not settle
+			const size_t smem = size_t(ctx->bp.t8.bytes) +
+			                    size_t(kPartialThreads / 32) * 2 * 20 * 32 * 4;
+			auto kern = ctx->bp.m <= 8
+			                ? partial_kernel<8>
+			                : (ctx->bp.m <= 16 ? partial_kernel<16> : partial_kernel<20>);
+			e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                         int(smem));
+			if (e != cudaSuccess)
+				return e;
+			kern<<<ctx->num_sms, kPartialThreads, smem, s>>>(X.P, ctx->bp);
+			BoundParams gbp = X.child_bp;
+			gbp.count_dev = &X.P.dev->n_unsettled;
+			gbp.gather = X.P.unsettled;
+			e = launch_pool_bounds(gbp, X.P.child_rec, X.child_cap, X.P.child_lb, 0,
+			                       ctx->num_sms, s);
+		} else {
+			FamilyArgs fa;
+			fa.fathers = X.P.tmp_rec;
+			fa.ridx = X.P.father_ridx;
+			fa.count_dev = &X.P.dev->n_fathers;
+			fa.child_off = X.P.child_off;
+			fa.child_lb = X.P.child_lb;
+			fa.child_job = X.P.child_job;
+			fa.stride = X.P.stride;
+			fa.fpairs = X.P.fpairs;
+			fa.K = X.P.K;
+			fa.ub_dev = &X.P.dev->ub;
+			fa.best_dev = &X.P.dev->best;
+			fa.early = &X.P.dev->early;
+			fa.settled_fathers = &X.P.dev->settled_fathers;
+			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms,
+			                      s);
+		}
 	} else {
 		if (X.mode == 2)
 			log_kernel<<<grid, 256, 0, s>>>(X.P);
@@ -1198,7 +1237,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 int window_min_of(int window) { return std::min(window, std::max(64, window / 64)); }
 
 void fill_stats(const wsbb::ExDev &h, const int16_t *best_rec, int n, int status,
-                double seconds, wsbb_stats *st)
+                double seconds, long long reads, int S, wsbb_stats *st)
 {
 	std::memset(st, 0, sizeof(*st));
 	st->branched = (int64_t)h.branched;
@@ -1219,6 +1258,8 @@ void fill_stats(const wsbb::ExDev &h, const int16_t *best_rec, int n, int status
 	st->scanned = (int64_t)h.scanned;
 	st->committed = (int64_t)h.committed;
 	st->early = (int64_t)h.early;
+	st->settled_fathers = (int64_t)h.settled_fathers;
+	st->d2h_bytes = (int64_t)(reads * (long long)sizeof(wsbb::ExDev) + S);
 }
 
 struct SearchMode {
@@ -1359,6 +1400,7 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	cudaEventCreate(&ev1);
 	cudaEventRecord(ev0, s);
 	ExDev h{};
+	long long reads = 0;
 	long long launched = 0;
 	const long long max_iters = cfg->max_iters > 0 ? cfg->max_iters : LLONG_MAX;
 	int status = 0;
@@ -1374,6 +1416,7 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 		if (e != cudaSuccess)
 			break;
 		e = cudaMemcpyAsync(&h, X->P.dev, sizeof(ExDev), cudaMemcpyDeviceToHost, s);
+		++reads;
 		if (e == cudaSuccess)
 			e = cudaStreamSynchronize(s);
 		if (e != cudaSuccess || h.done || h.error)
@@ -1395,7 +1438,7 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	e = cudaMemcpy(best_rec.data(), X->P.best_rec, S, cudaMemcpyDeviceToHost);
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "incumbent download");
-	fill_stats(h, best_rec.data(), n, status, ms * 1e-3, st);
+	fill_stats(h, best_rec.data(), n, status, ms * 1e-3, reads, S, st);
 	if (logged)
 		*logged = std::min((long long)h.log_count, M.log_cap);
 	if (h.error)
@@ -1533,6 +1576,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	const int G = cfg->graph_iters > 0 ? cfg->graph_iters : 16;
 	const long long max_iters = cfg->max_iters > 0 ? cfg->max_iters : LLONG_MAX;
 	ExDev h{};
+	long long reads = 0;
 	long long launched = 0;
 	int status = 0;
 	for (;;) {
@@ -1542,6 +1586,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 		if (e != cudaSuccess)
 			break;
 		e = cudaMemcpyAsync(&h, X.P.dev, sizeof(ExDev), cudaMemcpyDeviceToHost, s);
+		++reads;
 		if (e == cudaSuccess)
 			e = cudaStreamSynchronize(s);
 		if (e != cudaSuccess || h.done || h.error)
@@ -1561,7 +1606,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 		return ex_fail(ctx, e, "incumbent download");
 	const double secs =
 	    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-	fill_stats(h, best_rec, n, status, secs, st);
+	fill_stats(h, best_rec, n, status, secs, reads, S, st);
 	if (h.error)
 		return wsbb_set_error(ctx, h.error, "search outgrew the no-alloc scratch capacity");
 	return WSBB_OK;

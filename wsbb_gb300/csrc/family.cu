@@ -45,17 +45,22 @@ namespace wsbb {
 namespace {
 
 constexpr int kFamThreads = 256;
+constexpr int kFrontThreads = 64; // warps 0-1: fronts and backs, while the rest walk pairs
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
-__device__ __forceinline__ bool free_bit(const uint32_t (&mask)[4], int job)
+__device__ __forceinline__ bool free_bit(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
+                                         int job)
 {
-	return (mask[job >> 5] >> (job & 31)) & 1u;
+	const uint32_t lo = (job & 32) ? w1 : w0;
+	const uint32_t hi = (job & 32) ? w3 : w2;
+	return ((((job & 64) ? hi : lo) >> (job & 31)) & 1u) != 0;
 }
 
 struct FamLayout {
-	int xs;        // X row stride (odd: rows of consecutive pairs start in different banks)
-	int pc;        // pairs per chunk
-	size_t off_pairs, off_V, off_W, off_X, off_AB, off_red, off_F, off_G, off_fr, off_mask, bytes;
+	int xs; // X row stride (odd: rows of consecutive pairs start in different banks)
+	int pc; // pairs per chunk
+	size_t off_pairs, off_V, off_W, off_PF, off_PR, off_X, off_PI, off_red, off_F, off_G, off_fr,
+	    off_list, off_misc, bytes;
 };
 
 FamLayout fam_layout(int n, int m, int P, size_t budget)
@@ -63,40 +68,251 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 	FamLayout L;
 	L.xs = n | 1;
 	auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
-	size_t off = a16(size_t(m) * n * 4); // pt
+	size_t off = a16(size_t(m) * n * 2); // pt as uint16 (the tables cap times at 65535)
 	L.off_pairs = off;
 	off = a16(off + size_t(P) * 4);
 	L.off_V = off;
 	off = a16(off + size_t(m) * (n + 1) * 4);
 	L.off_W = off;
 	off = a16(off + size_t(m) * (n + 1) * 4);
-	const size_t fixed_after = a16(kFamThreads * 4) + a16(32 * 4) * 2 + a16((n + 4) * 2) + 16;
-	const size_t per_pair = size_t(L.xs) * 4 + 8;
+	L.off_PF = off;
+	off = a16(off + size_t(P) * 8);
+	L.off_PR = off;
+	off = a16(off + size_t(P) * 8);
+	const size_t fixed_after = a16(32 * 4) * 2 + a16(size_t(n + 4) * 2) + a16(size_t(2 * n) * 2) + 32;
+	const size_t per_pair = size_t(L.xs) * 4 + 16;
 	long long pc = budget > off + fixed_after ? (long long)((budget - off - fixed_after) / per_pair)
 	                                          : 0;
 	pc = std::max<long long>(pc, 32);
 	L.pc = int(std::min<long long>(pc, P));
+	// the per-thread reduction reuses the X rows once the pairs are consumed
 	L.off_X = off;
-	off = a16(off + size_t(L.pc) * L.xs * 4);
-	L.off_AB = off;
-	off = a16(off + size_t(L.pc) * 8);
 	L.off_red = off;
-	off = a16(off + kFamThreads * 4);
+	off = a16(off + std::max(size_t(L.pc) * L.xs * 4, size_t(2 * kFamThreads * 4)));
+	L.off_PI = off;
+	off = a16(off + size_t(L.pc) * 16);
 	L.off_F = off;
 	off = a16(off + 32 * 4);
 	L.off_G = off;
 	off = a16(off + 32 * 4);
 	L.off_fr = off;
 	off = a16(off + size_t(n + 4) * 2);
-	L.off_mask = off;
-	off += 16;
+	L.off_list = off;
+	off = a16(off + size_t(2 * n) * 2);
+	L.off_misc = off;
+	off += 32;
 	L.bytes = a16(off);
 	return L;
 }
 
-__global__ void __launch_bounds__(kFamThreads) family_lb2_kernel(FamilyArgs A, BoundParams bp,
-                                                                 const uint2 *__restrict__ tjT,
-                                                                 FamLayout L)
+struct FamSmem {
+	uint16_t *pt;
+	int32_t *pairs, *V, *W, *X, *red, *F, *G;
+	int2 *PF, *PR;
+	int4 *PI;
+	int16_t *fr, *list;
+	uint32_t *mask; // [4]
+	int *cnt;       // [1]
+};
+
+__device__ __forceinline__ FamSmem carve(uint8_t *smem, const FamLayout &L)
+{
+	FamSmem S;
+	S.pt = reinterpret_cast<uint16_t *>(smem);
+	S.pairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
+	S.V = reinterpret_cast<int32_t *>(smem + L.off_V);
+	S.W = reinterpret_cast<int32_t *>(smem + L.off_W);
+	S.PF = reinterpret_cast<int2 *>(smem + L.off_PF);
+	S.PR = reinterpret_cast<int2 *>(smem + L.off_PR);
+	S.X = reinterpret_cast<int32_t *>(smem + L.off_X);
+	S.PI = reinterpret_cast<int4 *>(smem + L.off_PI);
+	S.red = reinterpret_cast<int32_t *>(smem + L.off_red);
+	S.F = reinterpret_cast<int32_t *>(smem + L.off_F);
+	S.G = reinterpret_cast<int32_t *>(smem + L.off_G);
+	S.fr = reinterpret_cast<int16_t *>(smem + L.off_fr);
+	S.list = reinterpret_cast<int16_t *>(smem + L.off_list);
+	S.mask = reinterpret_cast<uint32_t *>(smem + L.off_misc);
+	S.cnt = reinterpret_cast<int *>(smem + L.off_misc + 16);
+	return S;
+}
+
+// Warp 0: the father's raw front F (a wavefront, lane = machine: lane k
+// takes job s - k at step s), the children's inherited front (column n of
+// V: F or the static heads), every BEGIN child's front (column j: F
+// followed by job j) and the per-pair (F[m1], F[m2]). Warp 1: the same for
+// the reversed back G, W and (back[m1] or -inf without back jobs, back[m2]).
+// With `leaves_only`, F and G only.
+__device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int lane, int n,
+                                                 int m, int P, int l1, int l2, int u,
+                                                 const int32_t *heads, const int32_t *tails,
+                                                 bool leaves_only)
+{
+	const int ld = n + 1;
+	if (warp == 0) {
+		int32_t Fk = 0;
+		const int nj = l1 + 1;
+		for (int s = 0; s < nj + m - 1; ++s) {
+			const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
+			const int i = s - lane;
+			if (lane < m && i >= 0 && i < nj)
+				Fk = max(Fk, lane > 0 ? left : 0) + S.pt[lane * n + S.fr[i]];
+		}
+		if (lane < m) {
+			S.F[lane] = Fk;
+			S.V[lane * ld + n] = l1 >= 0 ? Fk : heads[lane];
+		}
+		if (leaves_only)
+			return;
+		__syncwarp();
+		for (int i = lane; i < u; i += 32) {
+			const int j = S.fr[l1 + 1 + i];
+			int32_t v = 0;
+			for (int k = 0; k < m; ++k) {
+				v = max(v, S.F[k]) + S.pt[k * n + j];
+				S.V[k * ld + j] = v;
+			}
+		}
+		for (int p = lane; p < P; p += 32) {
+			const int pr = S.pairs[p];
+			S.PF[p] = make_int2(S.V[(pr & 0xff) * ld + n], S.V[(pr >> 8) * ld + n]);
+		}
+	} else if (warp == 1) {
+		int32_t Gq = 0;
+		const int nj = n - l2;
+		for (int s = 0; s < nj + m - 1; ++s) {
+			const int32_t left = __shfl_up_sync(0xffffffffu, Gq, 1);
+			const int i = s - lane;
+			if (lane < m && i >= 0 && i < nj)
+				Gq = max(Gq, lane > 0 ? left : 0) + S.pt[(m - 1 - lane) * n + S.fr[n - 1 - i]];
+		}
+		if (lane < m)
+			S.G[lane] = Gq;
+		if (leaves_only)
+			return;
+		__syncwarp();
+		if (lane < m)
+			S.W[lane * ld + n] = l2 < n ? S.G[m - 1 - lane] : tails[lane];
+		for (int i = lane; i < u; i += 32) {
+			const int j = S.fr[l1 + 1 + i];
+			int32_t g = 0;
+			for (int q = 0; q < m; ++q) {
+				g = max(g, S.G[q]) + S.pt[(m - 1 - q) * n + j];
+				S.W[(m - 1 - q) * ld + j] = g;
+			}
+		}
+		__syncwarp();
+		for (int p = lane; p < P; p += 32) {
+			const int pr = S.pairs[p];
+			const int32_t r1 = S.W[(pr & 0xff) * ld + n];
+			S.PR[p] = make_int2(l2 < n ? r1 : kNeg, S.W[(pr >> 8) * ld + n]);
+		}
+	}
+}
+
+constexpr int kWalkBatch = 8;
+
+// Pair p's forward and backward max-plus passes over its Johnson order,
+// restricted to the free jobs: X[slot][j] = C of (suffix after j) x
+// (prefix before j), and PI[slot] = (m1 | m2 << 8, A, B, p).
+__device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restrict__ tjT, int p,
+                                          int slot, int n, int P, int xs, uint32_t w0,
+                                          uint32_t w1, uint32_t w2, uint32_t w3)
+{
+	const uint2 *e = tjT + p;
+	int32_t *xrow = S.X + slot * xs;
+	int32_t a_sum = 0, b_sum = 0, c = kNeg;
+	for (int q0 = 0; q0 < n; q0 += kWalkBatch) {
+		uint2 v[kWalkBatch];
+#pragma unroll
+		for (int k = 0; k < kWalkBatch; ++k)
+			v[k] = q0 + k < n ? __ldg(e + (size_t)(q0 + k) * P) : make_uint2(0u, 0u);
+#pragma unroll
+		for (int k = 0; k < kWalkBatch; ++k) {
+			const int job = int(v[k].x & 0xffu);
+			if (q0 + k < n && free_bit(w0, w1, w2, w3, job)) {
+				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
+				const int32_t cj = a + int32_t(v[k].y >> 16) + b;
+				xrow[job] = c; // C of the prefix before job
+				c = max(c + b, a_sum + cj);
+				a_sum += a;
+				b_sum += b;
+			}
+		}
+	}
+	S.PI[slot] = make_int4(S.pairs[p], a_sum, b_sum, p);
+	int32_t as = 0, bs = 0, cs = kNeg;
+	for (int q0 = n - 1; q0 >= 0; q0 -= kWalkBatch) {
+		uint2 v[kWalkBatch];
+#pragma unroll
+		for (int k = 0; k < kWalkBatch; ++k)
+			v[k] = q0 - k >= 0 ? __ldg(e + (size_t)(q0 - k) * P) : make_uint2(0u, 0u);
+#pragma unroll
+		for (int k = 0; k < kWalkBatch; ++k) {
+			const int job = int(v[k].x & 0xffu);
+			if (q0 - k >= 0 && free_bit(w0, w1, w2, w3, job)) {
+				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
+				const int32_t cj = a + int32_t(v[k].y >> 16) + b;
+				const int32_t apre = a_sum - as - a;
+				xrow[job] = max(xrow[job] + bs, apre + cs);
+				cs = max(cs + a, bs + cj);
+				as += a;
+				bs += b;
+			}
+		}
+	}
+}
+
+// Both children that move job j (BEGIN and END) over chunk slots [lo, hi).
+__device__ __forceinline__ void job_pairs(const FamSmem &S, int lo, int hi, int j, int n, int xs,
+                                          int32_t &accB, int32_t &accE)
+{
+	const int ld = n + 1;
+	for (int t = lo; t < hi; ++t) {
+		const int4 pi = S.PI[t];
+		const int m1 = pi.x & 0xff, m2 = pi.x >> 8;
+		const int2 pf = S.PF[pi.w], pr = S.PR[pi.w];
+		const int32_t x = S.X[t * xs + j];
+		const int32_t aa = pi.y - S.pt[m1 * n + j], bb = pi.z - S.pt[m2 * n + j];
+		// BEGIN child: front V[.][j], the father's back
+		const int32_t v1 = S.V[m1 * ld + j], v2 = S.V[m2 * ld + j];
+		const int32_t t0 = v1 + aa, t1 = max(v2 + bb, v1 + x);
+		accB = max(accB, max(t1 + pr.y, t0 + pr.x));
+		// END child: the father's front, back W[.][j]
+		const int32_t w1 = S.W[m1 * ld + j], w2 = S.W[m2 * ld + j];
+		const int32_t e0 = pf.x + aa, e1 = max(pf.y + bb, pf.x + x);
+		accE = max(accE, max(e1 + w2, e0 + w1));
+	}
+}
+
+// One child (c < u: BEGIN, else END) over chunk slots [lo, hi).
+__device__ __forceinline__ int32_t child_pairs(const FamSmem &S, int lo, int hi, int j,
+                                               bool begin, int n, int xs, int32_t acc)
+{
+	const int ld = n + 1;
+	const int vcol = begin ? j : n, rcol = begin ? n : j;
+	for (int t = lo; t < hi; ++t) {
+		const int4 pi = S.PI[t];
+		const int m1 = pi.x & 0xff, m2 = pi.x >> 8;
+		const int32_t x = S.X[t * xs + j];
+		const int32_t aa = pi.y - S.pt[m1 * n + j], bb = pi.z - S.pt[m2 * n + j];
+		const int32_t v1 = S.V[m1 * ld + vcol], v2 = S.V[m2 * ld + vcol];
+		const int2 pr = S.PR[pi.w];
+		const int32_t r1 = begin ? pr.x : S.W[m1 * ld + rcol];
+		const int32_t r2 = begin ? pr.y : S.W[m2 * ld + rcol];
+		const int32_t t0 = v1 + aa, t1 = max(v2 + bb, v1 + x);
+		acc = max(acc, max(t1 + r2, t0 + r1));
+	}
+	return acc;
+}
+
+// kLearned: the father's K ranked pairs first; a child whose bound over
+// them reaches max(best, incumbent) is settled with that value (the search
+// only compares such bounds with the thresholds, never ranks or sums
+// them); fathers with children left walk every pair for those children.
+template <bool kLearned>
+__global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, BoundParams bp,
+                                                             const uint2 *__restrict__ tjT,
+                                                             FamLayout L)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
 	const long long nf = A.count_dev ? *A.count_dev : A.count;
@@ -104,28 +320,20 @@ __global__ void __launch_bounds__(kFamThreads) family_lb2_kernel(FamilyArgs A, B
 		return;
 	const int n = bp.n, m = bp.m, P = bp.P, xs = L.xs;
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	int32_t *s_pt = reinterpret_cast<int32_t *>(smem);
-	int32_t *s_pairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
-	int32_t *s_V = reinterpret_cast<int32_t *>(smem + L.off_V); // [m][n+1] child fronts
-	int32_t *s_W = reinterpret_cast<int32_t *>(smem + L.off_W); // [m][n+1] child backs
-	int32_t *s_X = reinterpret_cast<int32_t *>(smem + L.off_X); // [pc][xs]
-	int2 *s_AB = reinterpret_cast<int2 *>(smem + L.off_AB);     // [pc] (A, B)
-	int32_t *s_red = reinterpret_cast<int32_t *>(smem + L.off_red);
-	int32_t *s_F = reinterpret_cast<int32_t *>(smem + L.off_F); // father's raw front
-	int32_t *s_G = reinterpret_cast<int32_t *>(smem + L.off_G); // father's reversed back
-	int16_t *s_fr = reinterpret_cast<int16_t *>(smem + L.off_fr);
-	uint32_t *s_mask = reinterpret_cast<uint32_t *>(smem + L.off_mask);
+	const FamSmem S = carve(smem, L);
 	const uint8_t *tb = bp.t8.blob;
 	{
 		const int32_t *g_pt = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pt);
 		const int32_t *g_pairs = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pairs);
 		for (int i = tid; i < m * n; i += kFamThreads)
-			s_pt[i] = g_pt[i];
+			S.pt[i] = uint16_t(g_pt[i]);
 		for (int i = tid; i < P; i += kFamThreads)
-			s_pairs[i] = g_pairs[i];
+			S.pairs[i] = g_pairs[i];
 	}
 	const int32_t *heads = reinterpret_cast<const int32_t *>(tb + bp.t8.off_heads);
 	const int32_t *tails = reinterpret_cast<const int32_t *>(tb + bp.t8.off_tails);
+	const int thr = kLearned ? max(*A.best_dev, *A.ub_dev) : 0;
+	const int K = kLearned ? min(A.K, P) : 0;
 
 	for (long long f = blockIdx.x; f < nf; f += gridDim.x) {
 		const long long ri = A.ridx ? A.ridx[f] : f;
@@ -133,11 +341,13 @@ __global__ void __launch_bounds__(kFamThreads) family_lb2_kernel(FamilyArgs A, B
 		// job ids clamped to [0, n): a malformed record gives wrong bounds,
 		// never an access outside the tables
 		for (int i = tid; i < n + 2; i += kFamThreads)
-			s_fr[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
+			S.fr[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
 		if (tid < 4)
-			s_mask[tid] = 0;
+			S.mask[tid] = 0;
+		if (tid == 4)
+			*S.cnt = 0;
 		__syncthreads();
-		const int l1 = s_fr[n], l2 = s_fr[n + 1];
+		const int l1 = S.fr[n], l2 = S.fr[n + 1];
 		const int u = l2 - l1 - 1;
 		const long long c0 = A.child_off[f];
 		// cursors outside -1 <= l1, l2 <= n with two free jobs or more, or a
@@ -146,43 +356,17 @@ __global__ void __launch_bounds__(kFamThreads) family_lb2_kernel(FamilyArgs A, B
 			__syncthreads();
 			continue;
 		}
-		if (tid < u)
-			atomicOr(&s_mask[s_fr[l1 + 1 + tid] >> 5], 1u << (s_fr[l1 + 1 + tid] & 31));
-		// the father's raw front (warp 0) and reversed back (warp 1): a
-		// wavefront, lane = machine, lane k takes job s - k at step s
-		if (warp == 0) {
-			int32_t Fk = 0;
-			const int nj = l1 + 1;
-			for (int s = 0; s < nj + m - 1; ++s) {
-				const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
-				const int i = s - lane;
-				if (lane < m && i >= 0 && i < nj)
-					Fk = max(Fk, lane > 0 ? left : 0) + s_pt[lane * n + s_fr[i]];
-			}
-			if (lane < m)
-				s_F[lane] = Fk;
-		} else if (warp == 1) {
-			int32_t Gq = 0;
-			const int nj = n - l2;
-			for (int s = 0; s < nj + m - 1; ++s) {
-				const int32_t left = __shfl_up_sync(0xffffffffu, Gq, 1);
-				const int i = s - lane;
-				if (lane < m && i >= 0 && i < nj)
-					Gq = max(Gq, lane > 0 ? left : 0) + s_pt[(m - 1 - lane) * n + s_fr[n - 1 - i]];
-			}
-			if (lane < m)
-				s_G[lane] = Gq;
-		}
-		__syncthreads();
 		if (u == 2) {
-			// two leaves: makespan of front + (x, y) + back for both orders
+			// two leaves: makespans of front + (x, y) + back, both orders
+			fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, true);
+			__syncthreads();
 			if (tid < 2) {
-				const int x = s_fr[l1 + 1 + tid], y = s_fr[l1 + 2 - tid];
+				const int x = S.fr[l1 + 1 + tid], y = S.fr[l1 + 2 - tid];
 				int32_t v1 = 0, v2 = 0, mk = 0;
 				for (int k = 0; k < m; ++k) {
-					v1 = max(v1, s_F[k]) + s_pt[k * n + x];
-					v2 = max(v2, v1) + s_pt[k * n + y];
-					mk = max(mk, v2 + s_G[m - 1 - k]);
+					v1 = max(v1, S.F[k]) + S.pt[k * n + x];
+					v2 = max(v2, v1) + S.pt[k * n + y];
+					mk = max(mk, v2 + S.G[m - 1 - k]);
 				}
 				A.child_lb[c0 + tid] = mk;
 				A.child_job[c0 + tid] = int16_t(x);
@@ -190,102 +374,108 @@ __global__ void __launch_bounds__(kFamThreads) family_lb2_kernel(FamilyArgs A, B
 			__syncthreads();
 			continue;
 		}
-		uint32_t mask[4];
-#pragma unroll
-		for (int w = 0; w < 4; ++w)
-			mask[w] = s_mask[w];
-		// column n: what the children inherit (front for END children, back
-		// for BEGIN children, the static heads / tails when empty); column
-		// j: the BEGIN child's front / END child's back that moves job j
-		if (tid < m) {
-			s_V[tid * (n + 1) + n] = l1 >= 0 ? s_F[tid] : heads[tid];
-			s_W[tid * (n + 1) + n] = l2 < n ? s_G[m - 1 - tid] : tails[tid];
-		}
-		if (tid < u) {
-			const int j = s_fr[l1 + 1 + tid];
-			int32_t v = 0;
-			for (int k = 0; k < m; ++k) {
-				v = max(v, s_F[k]) + s_pt[k * n + j];
-				s_V[k * (n + 1) + j] = v;
-			}
-		} else if (tid >= 128 && tid - 128 < u) {
-			const int j = s_fr[l1 + 1 + tid - 128];
-			int32_t g = 0;
-			for (int q = 0; q < m; ++q) {
-				g = max(g, s_G[q]) + s_pt[(m - 1 - q) * n + j];
-				s_W[(m - 1 - q) * (n + 1) + j] = g;
-			}
-		}
-		// this thread's child and pair slice
-		const int nc = 2 * u, nc32 = (nc + 31) & ~31;
-		const int S = kFamThreads / nc32;
-		const int my_c = tid % nc32, my_s = tid / nc32;
-		const bool active = my_s < S && my_c < nc;
-		const bool begin = my_c < u;
-		const int my_j = active ? s_fr[l1 + 1 + (begin ? my_c : my_c - u)] : 0;
-		const int vcol = begin ? my_j : n, rcol = begin ? n : my_j;
-		const int32_t toff = (begin && l2 == n) ? kNeg : 0;
-		int32_t acc = kNeg;
-		for (int p_lo = 0; p_lo < P; p_lo += L.pc) {
-			const int len = min(L.pc, P - p_lo);
-			__syncthreads(); // fronts / backs written; previous chunk consumed
-			for (int t = tid; t < len; t += kFamThreads) {
-				const uint2 *e = tjT + p_lo + t;
-				int32_t *xrow = s_X + t * xs;
-				int32_t a_sum = 0, b_sum = 0, c = kNeg;
-				for (int q = 0; q < n; ++q) {
-					const uint2 v = __ldg(e + (size_t)q * P);
-					const int job = int(v.x & 0xffu);
-					if (free_bit(mask, job)) {
-						const int32_t a = int32_t(v.x >> 16), b = int32_t(v.y & 0xffffu);
-						const int32_t cj = a + int32_t(v.y >> 16) + b;
-						xrow[job] = c; // C of the prefix before job
-						c = max(c + b, a_sum + cj);
-						a_sum += a;
-						b_sum += b;
-					}
-				}
-				s_AB[t] = make_int2(a_sum, b_sum);
-				int32_t as = 0, bs = 0, cs = kNeg;
-				for (int q = n - 1; q >= 0; --q) {
-					const uint2 v = __ldg(e + (size_t)q * P);
-					const int job = int(v.x & 0xffu);
-					if (free_bit(mask, job)) {
-						const int32_t a = int32_t(v.x >> 16), b = int32_t(v.y & 0xffffu);
-						const int32_t cj = a + int32_t(v.y >> 16) + b;
-						const int32_t apre = a_sum - as - a;
-						xrow[job] = max(xrow[job] + bs, apre + cs);
-						cs = max(cs + a, bs + cj);
-						as += a;
-						bs += b;
-					}
-				}
-			}
-			__syncthreads();
-			if (active) {
-				const int lo = p_lo + my_s * len / S, hi = p_lo + (my_s + 1) * len / S;
-				for (int p = lo; p < hi; ++p) {
-					const int pr = s_pairs[p];
-					const int m1 = pr & 0xff, m2 = pr >> 8;
-					const int2 ab = s_AB[p - p_lo];
-					const int32_t x = s_X[(p - p_lo) * xs + my_j];
-					const int32_t a = s_pt[m1 * n + my_j], b = s_pt[m2 * n + my_j];
-					const int32_t v1 = s_V[m1 * (n + 1) + vcol], v2 = s_V[m2 * (n + 1) + vcol];
-					const int32_t r1 = s_W[m1 * (n + 1) + rcol], r2 = s_W[m2 * (n + 1) + rcol];
-					const int32_t t0 = v1 + ab.x - a;
-					const int32_t t1 = max(v2 + ab.y - b, v1 + x);
-					acc = max(acc, max(t1 + r2, t0 + r1 + toff));
-				}
-			}
-		}
-		s_red[tid] = acc;
+		if (tid < u)
+			atomicOr(&S.mask[S.fr[l1 + 1 + tid] >> 5], 1u << (S.fr[l1 + 1 + tid] & 31));
 		__syncthreads();
-		if (tid < nc) {
-			int32_t lb = s_red[tid];
-			for (int s = 1; s < S; ++s)
-				lb = max(lb, s_red[s * nc32 + tid]);
-			A.child_lb[c0 + tid] = lb;
-			A.child_job[c0 + tid] = int16_t(s_fr[l1 + 1 + (tid < u ? tid : tid - u)]);
+		const uint32_t w0 = S.mask[0], w1 = S.mask[1], w2 = S.mask[2], w3 = S.mask[3];
+		// first chunk: the K ranked pairs (learned) or pairs [0, pc); its
+		// walks overlap the fronts and backs
+		const int len0 = kLearned ? K : min(L.pc, P);
+		if (tid < kFrontThreads) {
+			fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, false);
+		} else {
+			for (int t = tid - kFrontThreads; t < len0; t += kFamThreads - kFrontThreads) {
+				int p = t;
+				if (kLearned)
+					p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
+				walk_pair(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
+			}
+		}
+		// per job: one thread per (job, slice of the chunk's pairs) takes
+		// both children that move the job
+		const int u32 = (u + 31) & ~31, NS = kFamThreads / u32;
+		const int my_i = tid % u32, my_s = tid / u32;
+		const bool active = my_s < NS && my_i < u;
+		const int my_j = active ? S.fr[l1 + 1 + my_i] : 0;
+		int32_t accB = kNeg, accE = kNeg;
+		__syncthreads();
+		if (active)
+			job_pairs(S, my_s * len0 / NS, (my_s + 1) * len0 / NS, my_j, n, xs, accB, accE);
+		if (!kLearned) {
+			for (int p_lo = len0; p_lo < P; p_lo += L.pc) {
+				const int len = min(L.pc, P - p_lo);
+				__syncthreads(); // previous chunk consumed
+				for (int t = tid; t < len; t += kFamThreads)
+					walk_pair(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+				__syncthreads();
+				if (active)
+					job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, n, xs, accB, accE);
+			}
+		}
+		__syncthreads(); // the reduction overwrites the X rows
+		S.red[2 * tid] = accB;
+		S.red[2 * tid + 1] = accE;
+		__syncthreads();
+		if (tid < u) {
+			int32_t lbB = S.red[2 * tid], lbE = S.red[2 * tid + 1];
+			for (int s = 1; s < NS; ++s) {
+				lbB = max(lbB, S.red[2 * (s * u32 + tid)]);
+				lbE = max(lbE, S.red[2 * (s * u32 + tid) + 1]);
+			}
+			const int16_t job = S.fr[l1 + 1 + tid];
+			A.child_job[c0 + tid] = job;
+			A.child_job[c0 + u + tid] = job;
+			if (!kLearned) {
+				A.child_lb[c0 + tid] = lbB;
+				A.child_lb[c0 + u + tid] = lbE;
+			} else {
+				// settled children keep the bound over the K pairs
+				if (lbB >= thr)
+					A.child_lb[c0 + tid] = lbB;
+				else
+					S.list[atomicAdd(S.cnt, 1)] = int16_t(tid);
+				if (lbE >= thr)
+					A.child_lb[c0 + u + tid] = lbE;
+				else
+					S.list[atomicAdd(S.cnt, 1)] = int16_t(u + tid);
+			}
+		}
+		if (kLearned) {
+			__syncthreads();
+			const int nu = *S.cnt;
+			if (tid == 0 && 2 * u - nu > 0)
+				atomicAdd(A.early, (unsigned long long)(2 * u - nu));
+			if (tid == 0 && nu == 0 && A.settled_fathers)
+				atomicAdd(A.settled_fathers, 1ull);
+			if (nu > 0) {
+				// the children left: every pair
+				const int nu32 = (nu + 31) & ~31, NS2 = kFamThreads / nu32;
+				const int ci = tid % nu32, cs = tid / nu32;
+				const bool act2 = cs < NS2 && ci < nu;
+				const int c = act2 ? S.list[ci] : 0;
+				const bool begin = c < u;
+				const int j = S.fr[l1 + 1 + (begin ? c : c - u)];
+				int32_t acc = kNeg;
+				for (int p_lo = 0; p_lo < P; p_lo += L.pc) {
+					const int len = min(L.pc, P - p_lo);
+					__syncthreads();
+					for (int t = tid; t < len; t += kFamThreads)
+						walk_pair(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+					__syncthreads();
+					if (act2)
+						acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, n,
+						                  xs, acc);
+				}
+				__syncthreads();
+				S.red[tid] = acc;
+				__syncthreads();
+				if (tid < nu) {
+					int32_t lb = S.red[tid];
+					for (int s = 1; s < NS2; ++s)
+						lb = max(lb, S.red[s * nu32 + tid]);
+					A.child_lb[c0 + S.list[tid]] = lb;
+				}
+			}
 		}
 		__syncthreads();
 	}
@@ -304,17 +494,18 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, cons
 	if (max_fathers <= 0)
 		return cudaSuccess;
 	const FamLayout L = fam_layout(bp.n, bp.m, bp.P, 56 * 1024);
-	cudaError_t e = cudaFuncSetAttribute(family_lb2_kernel,
-	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.bytes));
+	const bool learned = A.fpairs != nullptr;
+	auto kern = learned ? family_kernel<true> : family_kernel<false>;
+	cudaError_t e =
+	    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.bytes));
 	if (e != cudaSuccess)
 		return e;
 	int occ = 0;
-	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, family_lb2_kernel, kFamThreads,
-	                                                  L.bytes);
+	e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kFamThreads, L.bytes);
 	if (e != cudaSuccess)
 		return e;
 	const long long grid = std::min<long long>(max_fathers, (long long)num_sms * std::max(occ, 1));
-	family_lb2_kernel<<<unsigned(grid), kFamThreads, L.bytes, s>>>(A, bp, johnsonT, L);
+	kern<<<unsigned(grid), kFamThreads, L.bytes, s>>>(A, bp, johnsonT, L);
 	return cudaGetLastError();
 }
 

@@ -94,6 +94,14 @@ struct FamilyArgs {
 	int32_t *child_lb = nullptr;
 	int16_t *child_job = nullptr;        // the job each child moves
 	int stride = 0;                      // record stride in bytes
+	// learned form (fpairs set): father f's K ranked pairs fpairs[f * K ..];
+	// a child whose bound over them reaches max(*best_dev, *ub_dev) keeps
+	// that value (counted in *early), the others get their full LB2
+	const int16_t *fpairs = nullptr;
+	int K = 0;
+	const int *ub_dev = nullptr, *best_dev = nullptr;
+	unsigned long long *early = nullptr;
+	unsigned long long *settled_fathers = nullptr; // fathers with every child settled
 };
 cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, const FamilyArgs &A,
                               long long max_fathers, int num_sms, cudaStream_t s);

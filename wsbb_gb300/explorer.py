@@ -31,7 +31,8 @@ class ExploreStats(C.Structure):
                 ("discarded", C.c_int64), ("iterations", C.c_int64), ("best_cost", C.c_int32),
                 ("status", C.c_int32), ("depth_hist", C.c_uint64 * (MAX_JOBS + 1)),
                 ("best_perm", C.c_int32 * MAX_JOBS), ("seconds", C.c_double),
-                ("scanned", C.c_int64), ("committed", C.c_int64), ("early", C.c_int64)]
+                ("scanned", C.c_int64), ("committed", C.c_int64), ("early", C.c_int64),
+                ("settled_fathers", C.c_int64), ("d2h_bytes", C.c_int64)]
 
 
 NO_GRAPH = 1
@@ -65,4 +66,5 @@ def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int
             "best_cost": st.best_cost, "status": st.status,
             "coverage": coverage(st.depth_hist, n),
             "best_perm": np.array(st.best_perm[:n], dtype=np.int32),
-            "seconds": st.seconds, "scanned": st.scanned, "committed": st.committed}
+            "seconds": st.seconds, "scanned": st.scanned, "committed": st.committed,
+            "d2h_bytes": st.d2h_bytes}

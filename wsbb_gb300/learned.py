@@ -11,7 +11,7 @@ import numpy as np
 
 from ._lib import WsbbError, lib
 from .bound import Context
-from .explorer import INT32_MAX, ExploreCfg, ExploreStats, coverage
+from .explorer import CHILD_LB2, INT32_MAX, ExploreCfg, ExploreStats, coverage
 
 _declared = False
 
@@ -127,16 +127,18 @@ def _stats_dict(st: ExploreStats, n: int) -> dict:
             "discarded": st.discarded, "iterations": st.iterations,
             "best_cost": st.best_cost, "status": st.status,
             "coverage": coverage(st.depth_hist, n), "seconds": st.seconds,
-            "early": st.early, "best_perm": np.array(st.best_perm[:n], dtype=np.int32)}
+            "early": st.early, "settled_fathers": st.settled_fathers, "best_perm": np.array(st.best_perm[:n], dtype=np.int32)}
 
 
 def explore_learned(ctx: Context, model: Model, K: int, ub0: int | None = None,
                     best: int | None = None, window: int = 0, max_iters: int = 0,
-                    graph_iters: int = 0, stream: int = 0) -> dict:
-    """The exact search with the learned K-pair test; `best` defaults to ub0."""
+                    graph_iters: int = 0, stream: int = 0, child_lb2: bool = False) -> dict:
+    """The exact search with the learned K-pair test; `best` defaults to ub0.
+    `child_lb2`: the test and the full-LB2 fallback per child record (the
+    per-node kernels) instead of per father (family bounds)."""
     ub = INT32_MAX if ub0 is None else int(ub0)
     cfg = ExploreCfg(ub, int(ub if best is None else best), int(window), int(graph_iters), 0,
-                     int(max_iters), 0, 0)
+                     int(max_iters), CHILD_LB2 if child_lb2 else 0, 0)
     st = ExploreStats()
     rc = _L().wsbb_explore_learned(ctx.h, C.byref(cfg), model.h, int(K), C.byref(st),
                                    stream or None)

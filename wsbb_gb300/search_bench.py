@@ -65,8 +65,17 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
                 row["learned"][str(K)] = {
                     "seconds": q["seconds"], "early": q["early"],
                     "early_share": q["early"] / max(1, q["evaluated"]),
+                    "settled_fathers_share": q["settled_fathers"] / max(1, q["branched"]),
                     "same_tree": same, "speedup": r["seconds"] / max(q["seconds"], 1e-12),
                     "bounded_per_s": q["bounded"] / max(q["seconds"], 1e-12)}
+                if per_child:
+                    q2 = explore_learned(ctx, model, K, ub0=ub0, best=best, window=window,
+                                         max_iters=max_iters, child_lb2=True)
+                    row["learned"][str(K)]["per_child"] = {
+                        "seconds": q2["seconds"], "early": q2["early"],
+                        "same_tree": all(q2[k] == r[k] for k in TREE_KEYS),
+                        "speedup_vs_per_child": row["per_child"]["seconds"] /
+                        max(q2["seconds"], 1e-12)}
         runs.append(row)
         ctx.close()
         if verbose:
@@ -90,6 +99,13 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
                 "seconds": ls, "bounded_per_s": tot_b / max(ls, 1e-12),
                 "speedup_vs_plain": tot_s / max(ls, 1e-12),
                 "same_tree": all(r["learned"][str(K)]["same_tree"] for r in runs)}
+            if per_child:
+                lp = sum(r["learned"][str(K)]["per_child"]["seconds"] for r in runs)
+                out["learned"][str(K)]["per_child"] = {
+                    "seconds": lp, "bounded_per_s": tot_b / max(lp, 1e-12),
+                    "speedup_vs_per_child": out["per_child"]["seconds"] / max(lp, 1e-12),
+                    "same_tree": all(r["learned"][str(K)]["per_child"]["same_tree"]
+                                     for r in runs)}
     return out
 
 
