@@ -311,6 +311,21 @@ def proof_section() -> dict:
                              for r in out["runs"]]}
 
 
+def run_roofline_only() -> None:
+    """The roofline measurement alone: family bounds on the father pool."""
+    import ctypes as C
+
+    import torch
+
+    import wsbb_gb300 as W
+    dev = torch.device("cuda", 0)
+    ctx = W.Context(W.gen_instance(0, S_N, S_M))
+    stream = torch.cuda.current_stream(dev)
+    pk = C.c_double(0)
+    peak = pk.value if W.lib().wsbb_probe_maxplus_peak(0, C.byref(pk)) == 0 else None
+    print(json.dumps(roofline_family(ctx, dev, stream, stream.cuda_stream, peak)), flush=True)
+
+
 def run_gpu(args) -> None:
     import ctypes as C
 
@@ -331,22 +346,10 @@ def run_gpu(args) -> None:
         if world > 1:
             torch.distributed.barrier()
 
-    def reduce_max(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    from wsbb_gb300.replicas import aggregate, replica_seed
 
-    def reduce_sum(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        return float(t.item())
-
-    # replicas: rank r searches instance seed r (weak scaling)
-    seed = rank
+    # replicas: rank r searches its own instance (weak scaling)
+    seed = replica_seed(rank)
     p = W.gen_instance(seed, S_N, S_M)
     ub0, _ = W.neh(p)
     ctx = W.Context(p, device=local)
@@ -384,9 +387,8 @@ def run_gpu(args) -> None:
         torch.cuda.synchronize(dev)
         t_wall = time.perf_counter() - t_wall
     barrier()
-    total_ms = reduce_max(sum(a.elapsed_time(b) for a, b in ev))
-    all_bounded = reduce_sum(float(bounded))
-    value = all_bounded / (total_ms * 1e-3)
+    _, slow_s, value = aggregate(bounded, sum(a.elapsed_time(b) for a, b in ev) * 1e-3)
+    total_ms = slow_s * 1e3
     launches = args.steps * (ref["iterations"] * KERNELS_PER_ITER + 1)
 
     # end to end through the C-ABI from host memory
@@ -412,8 +414,7 @@ def run_gpu(args) -> None:
         d2h = int(st.d2h_bytes) + C.sizeof(st)
         e2e_bounded += st.bounded
         L.wsbb_ctx_destroy(h)
-    e2e_s = reduce_max(time.perf_counter() - t0)
-    e2e_value = reduce_sum(float(e2e_bounded)) / e2e_s
+    _, _, e2e_value = aggregate(e2e_bounded, time.perf_counter() - t0)
 
     arms = sections = cpu = roof = None
     if rank == 0:
@@ -474,7 +475,12 @@ def main():
     ap.add_argument("--impl", default="wsbb", choices=["wsbb", "reference"])
     ap.add_argument("--no-proof", action="store_true",
                     help="skip the time-to-proof section (n=50 m=10, seeds 0-4)")
+    ap.add_argument("--only", choices=["roofline"], default=None,
+                    help="run one measurement alone (a small case for profilers)")
     args = ap.parse_args()
+    if args.only == "roofline":
+        run_roofline_only()
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

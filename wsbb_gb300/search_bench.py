@@ -25,7 +25,7 @@ TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost",
 
 def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: str = "default",
         device: int = 0, verbose: bool = True, model_path: str = "", Ks=(8,),
-        per_child: bool = False) -> dict:
+        per_child: bool = False, capacity: int = 0) -> dict:
     """`per_child` also runs the search with every child bounded on its own
     (the per-node LB2 kernel) and reports its time and tree check."""
     model = None
@@ -39,7 +39,8 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
         ub0, _ = neh(p)
         ctx = Context(p, device=device)
         best = 99999 if best_mode == "default" else ub0
-        r = explore(ctx, ub0=ub0, best=best, window=window, max_iters=max_iters)
+        r = explore(ctx, ub0=ub0, best=best, window=window, max_iters=max_iters,
+                    capacity=capacity)
         row = {"n": n, "m": m, "seed": s, "neh": ub0, "best": best,
                "optimum": r["best_cost"], "proved": r["status"] == 0,
                "branched": r["branched"], "pruned": r["pruned"], "leaves": r["leaves"],
@@ -50,7 +51,7 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
                "bounded_per_s": r["bounded"] / max(r["seconds"], 1e-12)}
         if per_child:
             q = explore(ctx, ub0=ub0, best=best, window=window, max_iters=max_iters,
-                        child_lb2=True)
+                        child_lb2=True, capacity=capacity)
             row["per_child"] = {"seconds": q["seconds"],
                                 "same_tree": all(q[k] == r[k] for k in TREE_KEYS),
                                 "bounded_per_s": q["bounded"] / max(q["seconds"], 1e-12),
@@ -121,9 +122,11 @@ def main(argv=None) -> None:
     ap.add_argument("--K", type=int, nargs="+", default=[8])
     ap.add_argument("--per-child", action="store_true",
                     help="also search with per-child LB2 (the per-node kernel)")
+    ap.add_argument("--capacity", type=int, default=0,
+                    help="stack capacity in nodes (0: the library's default)")
     a = ap.parse_args(argv)
     out = run(a.n, a.m, a.seeds, a.window, a.max_iters, a.best, model_path=a.model, Ks=a.K,
-              per_child=a.per_child)
+              per_child=a.per_child, capacity=a.capacity)
     summary = {k: v for k, v in out.items() if k != "runs"}
     print(json.dumps({"summary": summary}), flush=True)
 
