@@ -71,8 +71,9 @@ size_t wsbb_node_stride(int n);
 /* Precompute the bound tables for an instance and upload them to `device`.
  * p_mxn[k*n + j] = processing time of job j on machine k (the reference's
  * machine-major stream order, src/instance_flowshop.cpp:88). Requires
- * 2 <= n <= 128, 2 <= m <= 32, 0 <= p <= 65535 and every machine-pair lag
- * (sum of p strictly between the two machines) <= 65535. */
+ * 2 <= n <= 128, 2 <= m <= 32, 0 <= p <= 65535 and, for every job and
+ * machine pair (m1, m2), p[m1] + lag + p[m2] <= 65535 (lag: the sum of p
+ * strictly between the two machines). */
 int wsbb_ctx_create(const int32_t *p_mxn, int n, int m, int device,
                     wsbb_ctx **out);
 void wsbb_ctx_destroy(wsbb_ctx *ctx);

@@ -87,6 +87,11 @@ def test_precompute_rejects_bad_sizes(W):
     assert W.lib().wsbb_precompute(p.ctypes.data, 5, 40, *(z.ctypes.data,) * 6) != 0
     p = np.ones((3, 200), dtype=np.int32)
     assert W.lib().wsbb_precompute(p.ctypes.data, 200, 3, *(z.ctypes.data,) * 6) != 0
+    # p1 + lag + p2 of a pair must fit 16 bits: 3 x 20000 fits, 3 x 30000 not
+    p = np.full((3, 4), 20000, dtype=np.int32)
+    assert W.lib().wsbb_precompute(p.ctypes.data, 4, 3, *(z.ctypes.data,) * 6) == 0
+    p = np.full((3, 4), 30000, dtype=np.int32)
+    assert W.lib().wsbb_precompute(p.ctypes.data, 4, 3, *(z.ctypes.data,) * 6) != 0
 
 
 def test_record_layout(W):

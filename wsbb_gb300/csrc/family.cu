@@ -48,10 +48,13 @@ constexpr int kFamThreads = 256;
 constexpr int kFrontThreads = 64; // warps 0-1: fronts and backs, while the rest walk pairs
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
+template <bool kWide>
 __device__ __forceinline__ bool free_bit(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
                                          int job)
 {
 	const uint32_t lo = (job & 32) ? w1 : w0;
+	if (!kWide) // n <= 64
+		return ((lo >> (job & 31)) & 1u) != 0;
 	const uint32_t hi = (job & 32) ? w3 : w2;
 	return ((((job & 64) ? hi : lo) >> (job & 31)) & 1u) != 0;
 }
@@ -68,7 +71,8 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 	FamLayout L;
 	L.xs = n | 1;
 	auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
-	size_t off = a16(size_t(m) * n * 2); // pt as uint16 (the tables cap times at 65535)
+	// pt as uint16 (the tables cap times at 65535), rows of n + 1 like V and W
+	size_t off = a16(size_t(m) * (n + 1) * 2);
 	L.off_pairs = off;
 	off = a16(off + size_t(P) * 4);
 	L.off_V = off;
@@ -155,7 +159,7 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 			const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
 			const int i = s - lane;
 			if (lane < m && i >= 0 && i < nj)
-				Fk = max(Fk, lane > 0 ? left : 0) + S.pt[lane * n + S.fr[i]];
+				Fk = max(Fk, lane > 0 ? left : 0) + S.pt[lane * ld + S.fr[i]];
 		}
 		if (lane < m) {
 			S.F[lane] = Fk;
@@ -168,7 +172,7 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 			const int j = S.fr[l1 + 1 + i];
 			int32_t v = 0;
 			for (int k = 0; k < m; ++k) {
-				v = max(v, S.F[k]) + S.pt[k * n + j];
+				v = max(v, S.F[k]) + S.pt[k * ld + j];
 				S.V[k * ld + j] = v;
 			}
 		}
@@ -183,7 +187,7 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 			const int32_t left = __shfl_up_sync(0xffffffffu, Gq, 1);
 			const int i = s - lane;
 			if (lane < m && i >= 0 && i < nj)
-				Gq = max(Gq, lane > 0 ? left : 0) + S.pt[(m - 1 - lane) * n + S.fr[n - 1 - i]];
+				Gq = max(Gq, lane > 0 ? left : 0) + S.pt[(m - 1 - lane) * ld + S.fr[n - 1 - i]];
 		}
 		if (lane < m)
 			S.G[lane] = Gq;
@@ -196,7 +200,7 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 			const int j = S.fr[l1 + 1 + i];
 			int32_t g = 0;
 			for (int q = 0; q < m; ++q) {
-				g = max(g, S.G[q]) + S.pt[(m - 1 - q) * n + j];
+				g = max(g, S.G[q]) + S.pt[(m - 1 - q) * ld + j];
 				S.W[(m - 1 - q) * ld + j] = g;
 			}
 		}
@@ -213,7 +217,9 @@ constexpr int kWalkBatch = 8;
 
 // Pair p's forward and backward max-plus passes over its Johnson order,
 // restricted to the free jobs: X[slot][j] = C of (suffix after j) x
-// (prefix before j), and PI[slot] = (m1 | m2 << 8, A, B, p).
+// (prefix before j), and PI[slot] = (m1 (n+1) | m2 (n+1) << 16, A, B, p):
+// the row offsets of the pair's machines in pt, V and W.
+template <bool kWide>
 __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restrict__ tjT, int p,
                                           int slot, int n, int P, int xs, uint32_t w0,
                                           uint32_t w1, uint32_t w2, uint32_t w3)
@@ -229,9 +235,9 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
 #pragma unroll
 		for (int k = 0; k < kWalkBatch; ++k) {
 			const int job = int(v[k].x & 0xffu);
-			if (q0 + k < n && free_bit(w0, w1, w2, w3, job)) {
+			if (q0 + k < n && free_bit<kWide>(w0, w1, w2, w3, job)) {
 				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
-				const int32_t cj = a + int32_t(v[k].y >> 16) + b;
+				const int32_t cj = int32_t(v[k].y >> 16); // a + lag + b
 				xrow[job] = c; // C of the prefix before job
 				c = max(c + b, a_sum + cj);
 				a_sum += a;
@@ -239,7 +245,8 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
 			}
 		}
 	}
-	S.PI[slot] = make_int4(S.pairs[p], a_sum, b_sum, p);
+	const int pr = S.pairs[p], ld = n + 1;
+	S.PI[slot] = make_int4((pr & 0xff) * ld | ((pr >> 8) * ld) << 16, a_sum, b_sum, p);
 	int32_t as = 0, bs = 0, cs = kNeg;
 	for (int q0 = n - 1; q0 >= 0; q0 -= kWalkBatch) {
 		uint2 v[kWalkBatch];
@@ -249,9 +256,9 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
 #pragma unroll
 		for (int k = 0; k < kWalkBatch; ++k) {
 			const int job = int(v[k].x & 0xffu);
-			if (q0 - k >= 0 && free_bit(w0, w1, w2, w3, job)) {
+			if (q0 - k >= 0 && free_bit<kWide>(w0, w1, w2, w3, job)) {
 				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
-				const int32_t cj = a + int32_t(v[k].y >> 16) + b;
+				const int32_t cj = int32_t(v[k].y >> 16);
 				const int32_t apre = a_sum - as - a;
 				xrow[job] = max(xrow[job] + bs, apre + cs);
 				cs = max(cs + a, bs + cj);
@@ -263,22 +270,22 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
 }
 
 // Both children that move job j (BEGIN and END) over chunk slots [lo, hi).
-__device__ __forceinline__ void job_pairs(const FamSmem &S, int lo, int hi, int j, int n, int xs,
+__device__ __forceinline__ void job_pairs(const FamSmem &S, int lo, int hi, int j, int xs,
                                           int32_t &accB, int32_t &accE)
 {
-	const int ld = n + 1;
-	for (int t = lo; t < hi; ++t) {
+	const int32_t *xp = S.X + lo * xs + j;
+	for (int t = lo; t < hi; ++t, xp += xs) {
 		const int4 pi = S.PI[t];
-		const int m1 = pi.x & 0xff, m2 = pi.x >> 8;
+		const int o1 = (pi.x & 0xffff) + j, o2 = (int(unsigned(pi.x) >> 16)) + j;
 		const int2 pf = S.PF[pi.w], pr = S.PR[pi.w];
-		const int32_t x = S.X[t * xs + j];
-		const int32_t aa = pi.y - S.pt[m1 * n + j], bb = pi.z - S.pt[m2 * n + j];
+		const int32_t x = *xp;
+		const int32_t aa = pi.y - int32_t(S.pt[o1]), bb = pi.z - int32_t(S.pt[o2]);
 		// BEGIN child: front V[.][j], the father's back
-		const int32_t v1 = S.V[m1 * ld + j], v2 = S.V[m2 * ld + j];
+		const int32_t v1 = S.V[o1], v2 = S.V[o2];
 		const int32_t t0 = v1 + aa, t1 = max(v2 + bb, v1 + x);
 		accB = max(accB, max(t1 + pr.y, t0 + pr.x));
 		// END child: the father's front, back W[.][j]
-		const int32_t w1 = S.W[m1 * ld + j], w2 = S.W[m2 * ld + j];
+		const int32_t w1 = S.W[o1], w2 = S.W[o2];
 		const int32_t e0 = pf.x + aa, e1 = max(pf.y + bb, pf.x + x);
 		accE = max(accE, max(e1 + w2, e0 + w1));
 	}
@@ -286,19 +293,18 @@ __device__ __forceinline__ void job_pairs(const FamSmem &S, int lo, int hi, int 
 
 // One child (c < u: BEGIN, else END) over chunk slots [lo, hi).
 __device__ __forceinline__ int32_t child_pairs(const FamSmem &S, int lo, int hi, int j,
-                                               bool begin, int n, int xs, int32_t acc)
+                                               bool begin, int xs, int32_t acc)
 {
-	const int ld = n + 1;
-	const int vcol = begin ? j : n, rcol = begin ? n : j;
-	for (int t = lo; t < hi; ++t) {
+	const int32_t *xp = S.X + lo * xs + j;
+	for (int t = lo; t < hi; ++t, xp += xs) {
 		const int4 pi = S.PI[t];
-		const int m1 = pi.x & 0xff, m2 = pi.x >> 8;
-		const int32_t x = S.X[t * xs + j];
-		const int32_t aa = pi.y - S.pt[m1 * n + j], bb = pi.z - S.pt[m2 * n + j];
-		const int32_t v1 = S.V[m1 * ld + vcol], v2 = S.V[m2 * ld + vcol];
-		const int2 pr = S.PR[pi.w];
-		const int32_t r1 = begin ? pr.x : S.W[m1 * ld + rcol];
-		const int32_t r2 = begin ? pr.y : S.W[m2 * ld + rcol];
+		const int o1 = (pi.x & 0xffff) + j, o2 = (int(unsigned(pi.x) >> 16)) + j;
+		const int32_t x = *xp;
+		const int32_t aa = pi.y - int32_t(S.pt[o1]), bb = pi.z - int32_t(S.pt[o2]);
+		const int2 pf = S.PF[pi.w], pr = S.PR[pi.w];
+		// BEGIN: own front, the father's back; END: the father's front, own back
+		const int32_t v1 = begin ? S.V[o1] : pf.x, v2 = begin ? S.V[o2] : pf.y;
+		const int32_t r1 = begin ? pr.x : S.W[o1], r2 = begin ? pr.y : S.W[o2];
 		const int32_t t0 = v1 + aa, t1 = max(v2 + bb, v1 + x);
 		acc = max(acc, max(t1 + r2, t0 + r1));
 	}
@@ -309,8 +315,8 @@ __device__ __forceinline__ int32_t child_pairs(const FamSmem &S, int lo, int hi,
 // them reaches max(best, incumbent) is settled with that value (the search
 // only compares such bounds with the thresholds, never ranks or sums
 // them); fathers with children left walk every pair for those children.
-template <bool kLearned>
-__global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, BoundParams bp,
+template <bool kLearned, bool kWide>
+__global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, BoundParams bp,
                                                              const uint2 *__restrict__ tjT,
                                                              FamLayout L)
 {
@@ -326,7 +332,7 @@ __global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, Bound
 		const int32_t *g_pt = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pt);
 		const int32_t *g_pairs = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pairs);
 		for (int i = tid; i < m * n; i += kFamThreads)
-			S.pt[i] = uint16_t(g_pt[i]);
+			S.pt[(i / n) * (n + 1) + i % n] = uint16_t(g_pt[i]);
 		for (int i = tid; i < P; i += kFamThreads)
 			S.pairs[i] = g_pairs[i];
 	}
@@ -364,8 +370,8 @@ __global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, Bound
 				const int x = S.fr[l1 + 1 + tid], y = S.fr[l1 + 2 - tid];
 				int32_t v1 = 0, v2 = 0, mk = 0;
 				for (int k = 0; k < m; ++k) {
-					v1 = max(v1, S.F[k]) + S.pt[k * n + x];
-					v2 = max(v2, v1) + S.pt[k * n + y];
+					v1 = max(v1, S.F[k]) + S.pt[k * (n + 1) + x];
+					v2 = max(v2, v1) + S.pt[k * (n + 1) + y];
 					mk = max(mk, v2 + S.G[m - 1 - k]);
 				}
 				A.child_lb[c0 + tid] = mk;
@@ -388,7 +394,7 @@ __global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, Bound
 				int p = t;
 				if (kLearned)
 					p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
-				walk_pair(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
+				walk_pair<kWide>(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
 			}
 		}
 		// per job: one thread per (job, slice of the chunk's pairs) takes
@@ -400,16 +406,16 @@ __global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, Bound
 		int32_t accB = kNeg, accE = kNeg;
 		__syncthreads();
 		if (active)
-			job_pairs(S, my_s * len0 / NS, (my_s + 1) * len0 / NS, my_j, n, xs, accB, accE);
+			job_pairs(S, my_s * len0 / NS, (my_s + 1) * len0 / NS, my_j, xs, accB, accE);
 		if (!kLearned) {
 			for (int p_lo = len0; p_lo < P; p_lo += L.pc) {
 				const int len = min(L.pc, P - p_lo);
 				__syncthreads(); // previous chunk consumed
 				for (int t = tid; t < len; t += kFamThreads)
-					walk_pair(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+					walk_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
 				__syncthreads();
 				if (active)
-					job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, n, xs, accB, accE);
+					job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, xs, accB, accE);
 			}
 		}
 		__syncthreads(); // the reduction overwrites the X rows
@@ -460,11 +466,11 @@ __global__ void __launch_bounds__(kFamThreads) family_kernel(FamilyArgs A, Bound
 					const int len = min(L.pc, P - p_lo);
 					__syncthreads();
 					for (int t = tid; t < len; t += kFamThreads)
-						walk_pair(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+						walk_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
 					__syncthreads();
 					if (act2)
-						acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, n,
-						                  xs, acc);
+						acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, xs,
+						                  acc);
 				}
 				__syncthreads();
 				S.red[tid] = acc;
@@ -495,7 +501,9 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, cons
 		return cudaSuccess;
 	const FamLayout L = fam_layout(bp.n, bp.m, bp.P, 56 * 1024);
 	const bool learned = A.fpairs != nullptr;
-	auto kern = learned ? family_kernel<true> : family_kernel<false>;
+	const bool wide = bp.n > 64;
+	auto kern = learned ? (wide ? family_kernel<true, true> : family_kernel<true, false>)
+	                    : (wide ? family_kernel<false, true> : family_kernel<false, false>);
 	cudaError_t e =
 	    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.bytes));
 	if (e != cudaSuccess)

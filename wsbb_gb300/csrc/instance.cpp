@@ -153,8 +153,8 @@ std::string build_instance(const int32_t *p, int n, int m, Instance &I)
 			for (int k = a + 1; k < b; ++k)
 				s += p[k * n + j];
 			lag[j] = s;
-			if (s > 65535)
-				return "machine-pair lags must be <= 65535";
+			if (s + p[a * n + j] + p[b * n + j] > 65535)
+				return "machine-pair sums p1 + lag + p2 must be <= 65535";
 			const bool first = p[a * n + j] < p[b * n + j];
 			cls[j] = first ? 1 : 2;
 			key[j] = (first ? p[a * n + j] : p[b * n + j]) + s;
@@ -224,14 +224,22 @@ HostTables pack_tables(const Instance &I, std::string &err)
 	H.img8 = pack_image(I, 8, H.t8);
 	if (I.n <= 32)
 		H.img16 = pack_image(I, 16, H.t16);
-	// position-major copy of the 8-byte Johnson entries
-	const size_t entries = size_t(I.P) * I.n;
-	H.imgT.resize(entries * 8);
-	const uint64_t *src = reinterpret_cast<const uint64_t *>(H.img8.data());
-	uint64_t *dst = reinterpret_cast<uint64_t *>(H.imgT.data());
-	for (int i = 0; i < I.P; ++i)
-		for (int q = 0; q < I.n; ++q)
-			dst[size_t(q) * I.P + i] = src[size_t(i) * I.n + q];
+	// position-major Johnson entries for the family bounds:
+	// x = job | p1 << 16, y = p2 | (p1 + lag + p2) << 16
+	const int n = I.n;
+	H.imgT.resize(size_t(I.P) * n * 8);
+	uint32_t *dst = reinterpret_cast<uint32_t *>(H.imgT.data());
+	for (int i = 0; i < I.P; ++i) {
+		const int a = I.mach0[i], b = I.mach1[i];
+		for (int q = 0; q < n; ++q) {
+			const int j = I.johnson[size_t(i) * n + q];
+			const uint32_t p1 = uint32_t(I.p[a * n + j]), p2 = uint32_t(I.p[b * n + j]);
+			const uint32_t c = p1 + uint32_t(I.lag[size_t(i) * n + j]) + p2;
+			const size_t e = size_t(q) * I.P + i;
+			dst[2 * e] = uint32_t(j) | (p1 << 16);
+			dst[2 * e + 1] = p2 | (c << 16);
+		}
+	}
 	if (H.t8.bytes > 200 * 1024)
 		err = "bound tables exceed the shared-memory budget (n * m too large)";
 	return H;
