@@ -4,9 +4,10 @@ per-child, learned and CPU arms on the same tree.
 Workload (one step = one search): permutation flowshop n = 50 jobs, m = 20
 machines (190 machine pairs), processing times uniform in [1, 99] from seed
 0; begin-end branching from the NEH incumbent with side-choice threshold
-best = NEH (the learned-selector configuration), 400 batched iterations of
-at most 16384 fathers each. Every step explores the same tree prefix (its
-counters are checked against the first step's). The search state grows to
+best = NEH (the learned-selector configuration), 400 batched iterations
+with the window and family-bounds tile the autotuner picks for this GPU
+(wsbb_gb300.autotune, untimed). Every step explores the same tree prefix
+(its counters are checked against the first step's). The search state grows to
 gigabytes over a step, far beyond the 129 MB L2; L2 is also flushed between
 steps.
 
@@ -63,7 +64,7 @@ PROOF_N, PROOF_M, PROOF_SEEDS = 50, 10, (0, 1, 2, 3, 4)
 def workload_config(seed: int, extra: dict | None = None) -> dict:
     cfg = {"workload": f"exact begin-end DFS, n={S_N} jobs m={S_M} machines (190 pairs), "
                        f"seed {seed}, NEH incumbent, best=NEH, {S_ITERS} batched iterations "
-                       "(window <= 16384 fathers) per step",
+                       "per step (autotuned window and tile)",
            "n": S_N, "m": S_M, "seed": seed, "iterations_per_step": S_ITERS,
            "l2": "search state >> L2 (GBs), L2 flushed between steps"}
     if extra:
@@ -357,8 +358,15 @@ def run_gpu(args) -> None:
     sptr = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
+    # launch shapes (window, family-bounds tile) from the autotuner: a short
+    # prefix of this search per candidate, untimed
+    from wsbb_gb300 import autotune
+    shape = autotune.tuned(ctx, ub0, ub0, device=local)
+    win, kb = shape["window"], shape["family_smem_kb"]
+
     def step():
-        return explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr)
+        return explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr, window=win,
+                       family_smem_kb=kb)
 
     ref = None
     for _ in range(args.warmup):
@@ -395,7 +403,7 @@ def run_gpu(args) -> None:
     L = W.lib()
     h_p = np.ascontiguousarray(p, dtype=np.int32)
     from wsbb_gb300.explorer import ExploreCfg, ExploreStats
-    cfg = ExploreCfg(ub0, ub0, 0, 0, 0, S_ITERS, 0, 0)
+    cfg = ExploreCfg(ub0, ub0, win, 0, 0, S_ITERS, 0, kb)
     e2e_steps = max(2, min(args.steps, 5))
     h2d = d2h = 0
     e2e_bounded = 0
@@ -423,14 +431,15 @@ def run_gpu(args) -> None:
                     "same_tree": all(r[k] == ref[k] for k in TREE_KEYS),
                     "speedup_vs_per_child_lb2": base_s / r["seconds"]}
         fam = step()
-        per = explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr, child_lb2=True)
+        per = explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr, child_lb2=True,
+                      window=win)
         arms = {"per_child_lb2": arm(per, per["seconds"]), "family_lb2": arm(fam, per["seconds"])}
         if os.path.exists(MODEL):
             model = Model(S_N, S_M)
             model.load(MODEL)
             for K, pc in ((16, True), (4, False)):
                 q = explore_learned(ctx, model, K, ub0=ub0, best=ub0, max_iters=S_ITERS,
-                                    stream=sptr, child_lb2=pc)
+                                    stream=sptr, child_lb2=pc, window=win)
                 a = arm(q, per["seconds"])
                 a["early_share"] = q["early"] / max(1, q["evaluated"])
                 a["settled_fathers_share"] = q["settled_fathers"] / max(1, q["branched"])
@@ -455,7 +464,9 @@ def run_gpu(args) -> None:
             "dtype": "int32", "data": "synthetic",
             "config": workload_config(seed, {"parallelism": f"replicas{world}",
                                              "bounded_per_step": ref["bounded"],
-                                             "same_tree_every_step": same}),
+                                             "same_tree_every_step": same,
+                                             "window": win, "family_smem_kb": kb,
+                                             "shapes": "autotuned (wsbb_gb300.autotune)"}),
             "roofline": roof, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps},

@@ -158,7 +158,10 @@ typedef struct {
 	                        16 window + 8192 */
 	int64_t max_iters;   /* stop after this many iterations (0: none) */
 	int32_t flags;       /* WSBB_EXPLORE_* */
-	int32_t reserved;
+	int32_t family_smem_kb; /* shared memory per CTA of the family bounds (KB,
+	                           0: 56): the pair-chunk length, and with it how
+	                           many CTAs share an SM (a tile shape the
+	                           autotuner picks) */
 } wsbb_explore_cfg;
 
 typedef struct {

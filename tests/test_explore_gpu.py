@@ -90,3 +90,23 @@ def test_capacity_error_is_reported(W):
     # the context stays usable
     got = E.explore(ctx, window=64)
     assert got["status"] == 0
+
+
+def test_autotuned_shapes_keep_the_tree():
+    """Every window / tile candidate of the autotuner explores the same tree."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import wsbb_gb300 as W
+    from wsbb_gb300 import autotune as A
+    from wsbb_gb300.explorer import explore
+    p = W.gen_instance(2, 20, 10)
+    ub, _ = W.neh(p)
+    ctx = W.Context(p)
+    choice, results = A.tune(ctx, ub, ub, iters=24, windows=(256, 2048), smem_kbs=(24, 56, 100))
+    assert choice in results and len(results) == 6
+    assert len({r["bounded"] for r in results if r["window"] == 2048}) == 1
+    full = [explore(ctx, ub0=ub, best=ub, window=r["window"], family_smem_kb=r["family_smem_kb"])
+            for r in results]
+    keys = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost", "coverage")
+    assert all(all(f[k] == full[0][k] for k in keys) for f in full)

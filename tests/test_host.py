@@ -129,3 +129,20 @@ def test_child_order_partitions_the_permutations(W):
             assert int(k[n + 2]) == int(r[n + 2]) + 1
             stack.append(k)
     assert len(leaves) == 720 and len(set(leaves)) == 720
+
+
+def test_autotune_cache_and_pick(tmp_path, monkeypatch):
+    from wsbb_gb300 import autotune as A
+    monkeypatch.setenv("WSBB_GB300_CACHE", str(tmp_path))
+    rs = [{"window": 4096, "family_smem_kb": 56, "bounded_per_s": 10.0},
+          {"window": 8192, "family_smem_kb": 100, "bounded_per_s": 12.05},
+          {"window": 2048, "family_smem_kb": 56, "bounded_per_s": 12.0}]
+    assert A.pick(rs) == rs[2]  # within 1 %: the smaller tile and window
+    assert A.pick(rs, tolerance=0.0) == rs[1]
+    key = A.cache_key("GB300", 50, 20, True)
+    assert A.load_cache() == {}
+    A.store(key, rs[1])
+    A.store(A.cache_key("GB300", 20, 20, False), rs[0])
+    data = A.load_cache()
+    assert data[key] == rs[1] and len(data) == 2
+    assert A.cache_path().startswith(str(tmp_path))

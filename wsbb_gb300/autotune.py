@@ -1,0 +1,114 @@
+"""Autotuner for the search's launch shapes.
+
+Two shapes set how the batched search maps onto the GPU:
+  window          fathers branched per iteration (the batch: more work per
+                  launch against more speculative work)
+  family_smem_kb  shared memory per CTA of the family bounds: how many
+                  machine pairs one chunk holds (their per-job X rows) and
+                  with it how many CTAs share an SM
+Neither changes the tree. `tune` times a short prefix of the search for
+every candidate pair and keeps the one with the most bounded nodes per
+second; `tuned` caches the choice per (GPU, n, m, best mode) in
+~/.cache/wsbb_gb300/autotune.json (WSBB_GB300_CACHE overrides the folder).
+
+    python -m wsbb_gb300.autotune --n 50 --m 20 --best ub0
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+WINDOWS = (2048, 4096, 8192, 16384, 32768)
+SMEM_KB = (56, 100, 160)
+
+
+def cache_path() -> str:
+    root = os.environ.get("WSBB_GB300_CACHE") or os.path.join(
+        os.path.expanduser("~"), ".cache", "wsbb_gb300")
+    return os.path.join(root, "autotune.json")
+
+
+def cache_key(device_name: str, n: int, m: int, best_is_ub: bool) -> str:
+    return f"{device_name}|n={n}|m={m}|best={'ub0' if best_is_ub else 'default'}"
+
+
+def load_cache(path: str | None = None) -> dict:
+    path = path or cache_path()
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def store(key: str, choice: dict, path: str | None = None) -> None:
+    path = path or cache_path()
+    data = load_cache(path)
+    data[key] = choice
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def pick(results: list[dict], tolerance: float = 0.01) -> dict:
+    """The fastest candidate; candidates within `tolerance` of it count as
+    ties (timing noise), and among those the smallest tile, then the
+    smallest window wins (less memory, less speculation)."""
+    top = max(r["bounded_per_s"] for r in results)
+    near = [r for r in results if r["bounded_per_s"] >= top * (1 - tolerance)]
+    return min(near, key=lambda r: (r["family_smem_kb"], r["window"]))
+
+
+def tune(ctx, ub0: int, best: int, iters: int = 96, windows=WINDOWS, smem_kbs=SMEM_KB,
+         capacity: int = 0, stream: int = 0) -> tuple[dict, list[dict]]:
+    from .explorer import explore
+    results = []
+    for w in windows:
+        for kb in smem_kbs:
+            r = explore(ctx, ub0=ub0, best=best, window=w, max_iters=iters, capacity=capacity,
+                        family_smem_kb=kb, stream=stream)
+            results.append({"window": w, "family_smem_kb": kb, "iterations": r["iterations"],
+                            "bounded": r["bounded"], "seconds": r["seconds"],
+                            "bounded_per_s": r["bounded"] / max(r["seconds"], 1e-12)})
+    return pick(results), results
+
+
+def tuned(ctx, ub0: int, best: int, device: int = 0, retune: bool = False, **kw) -> dict:
+    """The cached choice for this GPU and instance shape, tuning on a miss."""
+    import torch
+    name = torch.cuda.get_device_name(device)
+    key = cache_key(name, ctx.n, ctx.m, best == ub0)
+    if not retune:
+        hit = load_cache().get(key)
+        if hit:
+            return dict(hit, cached=True)
+    choice, _ = tune(ctx, ub0, best, **kw)
+    store(key, choice)
+    return dict(choice, cached=False)
+
+
+def main(argv=None) -> None:
+    from .bound import Context, gen_instance, neh
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=50)
+    ap.add_argument("--m", type=int, default=20)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--best", default="ub0", choices=["default", "ub0"])
+    ap.add_argument("--iters", type=int, default=96)
+    a = ap.parse_args(argv)
+    p = gen_instance(a.seed, a.n, a.m)
+    ub0, _ = neh(p)
+    ctx = Context(p)
+    best = ub0 if a.best == "ub0" else 99999
+    choice, results = tune(ctx, ub0, best, iters=a.iters)
+    import torch
+    store(cache_key(torch.cuda.get_device_name(0), a.n, a.m, a.best == "ub0"), choice)
+    print(json.dumps({"choice": choice, "candidates": results}), flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1123,6 +1123,7 @@ struct ExploreState {
 	// per father (family bounds)
 	bool child_lb2 = false;
 	bool graph_child_lb2 = false;
+	int fam_kb = 0, graph_fam_kb = 0; // family bounds' shared-memory budget
 };
 
 void wsbb_explore_release(wsbb_ctx *ctx)
@@ -1203,7 +1204,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			fa.early = &X.P.dev->early;
 			fa.settled_fathers = &X.P.dev->settled_fathers;
 			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms,
-			                      s);
+			                      s, X.fam_kb);
 		}
 	} else {
 		if (X.mode == 2)
@@ -1220,7 +1221,8 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			fa.child_lb = X.P.child_lb;
 			fa.child_job = X.P.child_job;
 			fa.stride = X.P.stride;
-			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms, s);
+			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms, s,
+			                      X.fam_kb);
 		}
 	}
 	if (e != cudaSuccess)
@@ -1361,8 +1363,9 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	// kernel arguments are captured by value: any change of mode, model, K,
 	// learned buffers or log target needs a new graph
 	X->child_lb2 = (cfg->flags & WSBB_EXPLORE_CHILD_LB2) != 0;
+	X->fam_kb = cfg->family_smem_kb;
 	const bool stale = X->graph_iters != G || X->graph_stream != s || X->mode != M.mode ||
-	                   X->graph_child_lb2 != X->child_lb2 ||
+	                   X->graph_child_lb2 != X->child_lb2 || X->graph_fam_kb != X->fam_kb ||
 	                   X->model != M.model || X->graph_K != X->P.K ||
 	                   X->graph_learned != X->learned_mem || X->graph_log != X->P.log_rec ||
 	                   X->graph_log_cap != X->P.log_cap || X->graph_log_stride != X->P.log_stride;
@@ -1374,6 +1377,7 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	X->graph_log_cap = X->P.log_cap;
 	X->graph_log_stride = X->P.log_stride;
 	X->graph_child_lb2 = X->child_lb2;
+	X->graph_fam_kb = X->fam_kb;
 	if (use_graph && (!X->graph || stale)) {
 		if (X->graph)
 			cudaGraphExecDestroy(X->graph);
@@ -1566,6 +1570,7 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	X.child_bp = ctx->bp;
 	X.child_bp.count_dev = &X.P.dev->n_children;
 	X.child_lb2 = (cfg->flags & WSBB_EXPLORE_CHILD_LB2) != 0;
+	X.fam_kb = cfg->family_smem_kb;
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
 	const auto t0 = std::chrono::steady_clock::now();

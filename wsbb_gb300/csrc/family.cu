@@ -489,17 +489,18 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 
 }  // namespace
 
-size_t family_smem(const BoundParams &bp)
+size_t family_smem(const BoundParams &bp, int smem_kb)
 {
-	return fam_layout(bp.n, bp.m, bp.P, 56 * 1024).bytes;
+	return fam_layout(bp.n, bp.m, bp.P, size_t(smem_kb > 0 ? smem_kb : 56) * 1024).bytes;
 }
 
 cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, const FamilyArgs &A,
-                              long long max_fathers, int num_sms, cudaStream_t s)
+                              long long max_fathers, int num_sms, cudaStream_t s, int smem_kb)
 {
 	if (max_fathers <= 0)
 		return cudaSuccess;
-	const FamLayout L = fam_layout(bp.n, bp.m, bp.P, 56 * 1024);
+	const size_t budget = size_t(std::min(std::max(smem_kb > 0 ? smem_kb : 56, 16), 220)) * 1024;
+	const FamLayout L = fam_layout(bp.n, bp.m, bp.P, budget);
 	const bool learned = A.fpairs != nullptr;
 	const bool wide = bp.n > 64;
 	auto kern = learned ? (wide ? family_kernel<true, true> : family_kernel<true, false>)

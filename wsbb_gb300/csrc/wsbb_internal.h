@@ -103,9 +103,12 @@ struct FamilyArgs {
 	unsigned long long *early = nullptr;
 	unsigned long long *settled_fathers = nullptr; // fathers with every child settled
 };
+// smem_kb: shared-memory budget per CTA in KB (0: 56), which sets the
+// pair-chunk length and how many CTAs share an SM.
 cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, const FamilyArgs &A,
-                              long long max_fathers, int num_sms, cudaStream_t s);
-size_t family_smem(const BoundParams &bp);
+                              long long max_fathers, int num_sms, cudaStream_t s,
+                              int smem_kb = 0);
+size_t family_smem(const BoundParams &bp, int smem_kb = 0);
 
 // Learned selector inference (learned.cu): top-K pairs of `rows` feature
 // rows (rows_dev, when set, holds the row count on the device).
