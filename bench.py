@@ -28,8 +28,9 @@ steps.
          in this run
   cpu_baseline / --impl reference: the CPU port of the reference explorer
          (oracle/, its semantics and counters) on the host cores
-Sections: the LB2 pool kernel (n=20 m=20 pools of 2^20 records) and the
-time-to-proof of the n=50 m=10 instances (seeds 0-4).
+Sections: the LB2 pool kernel (n=20 m=20 pools of 2^20 records), the
+time-to-proof of the n=50 m=10 instances (seeds 0-4) and 64 mixed instances
+searched concurrently (wsbb_gb300.multi_bench).
 """
 from __future__ import annotations
 
@@ -448,6 +449,12 @@ def run_gpu(args) -> None:
         sections = {"lb2_pool": lb2_pool_section(dev, stream, sptr, peak, 40)}
         if not args.no_proof:
             sections["time_to_proof"] = proof_section()
+        if not args.no_multi:
+            from wsbb_gb300 import multi_bench
+            sections["multi_instance"] = multi_bench.run()
+            sections["multi_instance"]["workload"] = (
+                "64 instances, n in {20,50,100} x m in {5,10,20}, seeds 0-63, NEH incumbent, "
+                "best=NEH, one context and stream each, 8 host threads, <= 64 iterations each")
         if world == 1:
             cores = os.cpu_count() or 1
             cpu = cpu_search_rate(0, cores, 8.0)
@@ -486,6 +493,8 @@ def main():
     ap.add_argument("--impl", default="wsbb", choices=["wsbb", "reference"])
     ap.add_argument("--no-proof", action="store_true",
                     help="skip the time-to-proof section (n=50 m=10, seeds 0-4)")
+    ap.add_argument("--no-multi", action="store_true",
+                    help="skip the multi-instance section (64 concurrent instances)")
     ap.add_argument("--only", choices=["roofline"], default=None,
                     help="run one measurement alone (a small case for profilers)")
     args = ap.parse_args()

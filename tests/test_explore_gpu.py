@@ -110,3 +110,18 @@ def test_autotuned_shapes_keep_the_tree():
             for r in results]
     keys = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost", "coverage")
     assert all(all(f[k] == full[0][k] for k in keys) for f in full)
+
+
+def test_concurrent_searches_on_many_contexts():
+    """Searches on several contexts from several host threads at once (their
+    graph captures overlap): every arm completes with the same trees."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from wsbb_gb300 import multi_bench
+    out = multi_bench.run(instances=9, threads=3, max_iters=16, window=512,
+                          arms=("family", "per_child"))
+    for arm in ("family", "per_child"):
+        a = out["arms"][arm]
+        assert a["instances"] == 9 and a["same_tree"], arm
+    assert out["arms"]["family"]["bounded"] == out["arms"]["per_child"]["bounded"] > 0

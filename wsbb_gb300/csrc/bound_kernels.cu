@@ -457,8 +457,7 @@ template <typename K>
 cudaError_t launch(K kernel, int threads, size_t smem, const BoundParams &bp, const void *recs,
                    int64_t count, int32_t *out, int num_sms, cudaStream_t stream)
 {
-	cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-	                                     int(smem));
+	cudaError_t e = allow_max_dynamic_smem(kernel);
 	if (e != cudaSuccess)
 		return e;
 	int per_sm = 0;

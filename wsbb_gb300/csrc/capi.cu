@@ -4,6 +4,10 @@
 #include <cstring>
 #include <new>
 
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "wsbb_internal.h"
 
 int wsbb_set_error(wsbb_ctx *ctx, int code, const std::string &msg)
@@ -126,6 +130,28 @@ extern "C" void wsbb_ctx_destroy(wsbb_ctx *ctx)
 		cudaStreamDestroy(ctx->stream);
 	delete ctx;
 }
+
+namespace wsbb {
+cudaError_t allow_max_dynamic_smem_fn(const void *kernel)
+{
+	static std::mutex mu;
+	static std::set<std::pair<int, const void *>> done;
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess)
+		return e;
+	std::lock_guard<std::mutex> lock(mu);
+	if (done.count({dev, kernel}))
+		return cudaSuccess;
+	int max_optin = 0;
+	e = cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin);
+	if (e == cudaSuccess)
+		done.insert({dev, kernel});
+	return e;
+}
+}  // namespace wsbb
 
 extern "C" size_t wsbb_ctx_device_bytes(const wsbb_ctx *ctx)
 {

@@ -1178,8 +1178,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			auto kern = ctx->bp.m <= 8
 			                ? partial_kernel<8>
 			                : (ctx->bp.m <= 16 ? partial_kernel<16> : partial_kernel<20>);
-			e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                         int(smem));
+			e = allow_max_dynamic_smem(kern);
 			if (e != cudaSuccess)
 				return e;
 			kern<<<ctx->num_sms, kPartialThreads, smem, s>>>(X.P, ctx->bp);

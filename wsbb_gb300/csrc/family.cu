@@ -505,8 +505,7 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, cons
 	const bool wide = bp.n > 64;
 	auto kern = learned ? (wide ? family_kernel<true, true> : family_kernel<true, false>)
 	                    : (wide ? family_kernel<false, true> : family_kernel<false, false>);
-	cudaError_t e =
-	    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(L.bytes));
+	cudaError_t e = allow_max_dynamic_smem(kern);
 	if (e != cudaSuccess)
 		return e;
 	int occ = 0;

@@ -805,8 +805,7 @@ cudaError_t launch_mlp_topk(const wsbb_model *md, const float *X, long long rows
 	a.topk = topk;
 	a.logits = logits;
 	const size_t smem = size_t(kInferWarps) * infer_warp_bytes(md->D, md->O);
-	cudaError_t e = cudaFuncSetAttribute(mlp_infer_kernel,
-	                                     cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+	cudaError_t e = allow_max_dynamic_smem(mlp_infer_kernel);
 	if (e != cudaSuccess)
 		return e;
 	const long long tiles = (rows + 15) / 16;

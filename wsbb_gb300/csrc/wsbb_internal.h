@@ -49,9 +49,9 @@ struct DeviceTables {
 	void *mem = nullptr; // all images in one allocation
 	size_t bytes = 0;
 	TableView t8, t16;   // t16.blob is null when n > 32
-	// The 8-byte Johnson entries position-major, johnsonT[q * P + i] = entry
-	// q of pair i, so that threads walking consecutive pairs read
-	// consecutive entries (family bounds).
+	// Johnson entries position-major, johnsonT[q * P + i] = entry q of pair
+	// i, so that threads walking consecutive pairs read consecutive entries
+	// (family bounds): x = job | p1 << 16, y = p2 | (p1 + lag + p2) << 16.
 	const uint2 *johnsonT = nullptr;
 };
 
@@ -115,6 +115,18 @@ size_t family_smem(const BoundParams &bp, int smem_kb = 0);
 cudaError_t launch_mlp_topk(const wsbb_model *md, const float *X, long long rows,
                             const long long *rows_dev, int K, int16_t *topk, float *logits,
                             int num_sms, cudaStream_t s);
+
+// Raises a kernel's dynamic shared-memory ceiling to the device's opt-in
+// maximum, once per (device, kernel). The ceiling is process-wide per
+// function, so setting it to each launch's own size would let one host
+// thread lower it under another thread's launch (which then fails); the
+// ceiling itself changes neither occupancy nor the launch.
+cudaError_t allow_max_dynamic_smem_fn(const void *kernel);
+template <typename K>
+cudaError_t allow_max_dynamic_smem(K kernel)
+{
+	return allow_max_dynamic_smem_fn(reinterpret_cast<const void *>(kernel));
+}
 
 // Orders the library's own stream `s` after the work already queued on the
 // legacy default stream, where a caller given no stream (PyTorch's default
