@@ -70,7 +70,7 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 	}
 	ctx->device = device;
 	wsbb::DeviceTables &T = ctx->tables;
-	T.bytes = H.img8.size() + H.img16.size() + H.imgT.size();
+	T.bytes = H.img8.size() + H.img16.size() + H.imgT.size() + H.imgPos.size();
 	cudaError_t e = cudaSetDevice(device);
 	if (e == cudaSuccess)
 		e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
@@ -86,6 +86,9 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 		e = cudaMemcpy(base + H.img8.size() + H.img16.size(), H.imgT.data(), H.imgT.size(),
 		               cudaMemcpyHostToDevice);
 	if (e == cudaSuccess)
+		e = cudaMemcpy(base + H.img8.size() + H.img16.size() + H.imgT.size(), H.imgPos.data(),
+		               H.imgPos.size(), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess)
 		e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
 	if (e != cudaSuccess) {
 		fprintf(stderr, "wsbb_ctx_create: %s\n", cudaGetErrorString(e));
@@ -97,6 +100,7 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 	T.t16 = H.t16;
 	T.t16.blob = H.img16.empty() ? nullptr : base + H.img8.size();
 	T.johnsonT = reinterpret_cast<const uint2 *>(base + H.img8.size() + H.img16.size());
+	T.jobposT = base + H.img8.size() + H.img16.size() + H.imgT.size();
 	wsbb::BoundParams &bp = ctx->bp;
 	bp.t8 = T.t8;
 	bp.t16 = T.t16;

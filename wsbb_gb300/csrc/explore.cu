@@ -1202,7 +1202,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			fa.best_dev = &X.P.dev->best;
 			fa.early = &X.P.dev->early;
 			fa.settled_fathers = &X.P.dev->settled_fathers;
-			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms,
+			e = launch_family_lb2(ctx->bp, ctx->tables, fa, X.window, ctx->num_sms,
 			                      s, X.fam_kb);
 		}
 	} else {
@@ -1220,7 +1220,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			fa.child_lb = X.P.child_lb;
 			fa.child_job = X.P.child_job;
 			fa.stride = X.P.stride;
-			e = launch_family_lb2(ctx->bp, ctx->tables.johnsonT, fa, X.window, ctx->num_sms, s,
+			e = launch_family_lb2(ctx->bp, ctx->tables, fa, X.window, ctx->num_sms, s,
 			                      X.fam_kb);
 		}
 	}

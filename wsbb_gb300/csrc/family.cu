@@ -48,17 +48,6 @@ constexpr int kFamThreads = 256;
 constexpr int kFrontThreads = 64; // warps 0-1: fronts and backs, while the rest walk pairs
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
-template <bool kWide>
-__device__ __forceinline__ bool free_bit(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
-                                         int job)
-{
-	const uint32_t lo = (job & 32) ? w1 : w0;
-	if (!kWide) // n <= 64
-		return ((lo >> (job & 31)) & 1u) != 0;
-	const uint32_t hi = (job & 32) ? w3 : w2;
-	return ((((job & 64) ? hi : lo) >> (job & 31)) & 1u) != 0;
-}
-
 struct FamLayout {
 	int xs; // X row stride (odd: rows of consecutive pairs start in different banks)
 	int pc; // pairs per chunk
@@ -115,7 +104,6 @@ struct FamSmem {
 	int2 *PF, *PR;
 	int4 *PI;
 	int16_t *fr, *list;
-	uint32_t *mask; // [4]
 	int *cnt;       // [1]
 };
 
@@ -135,7 +123,6 @@ __device__ __forceinline__ FamSmem carve(uint8_t *smem, const FamLayout &L)
 	S.G = reinterpret_cast<int32_t *>(smem + L.off_G);
 	S.fr = reinterpret_cast<int16_t *>(smem + L.off_fr);
 	S.list = reinterpret_cast<int16_t *>(smem + L.off_list);
-	S.mask = reinterpret_cast<uint32_t *>(smem + L.off_misc);
 	S.cnt = reinterpret_cast<int *>(smem + L.off_misc + 16);
 	return S;
 }
@@ -213,29 +200,79 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 	}
 }
 
-constexpr int kWalkBatch = 8;
+constexpr int kWalkBatch = 4;
+
+// The next free position of a pair's Johnson order (ascending or
+// descending) from its free-position mask (w0: positions 0-63, w1: 64-127);
+// -1 when none is left.
+template <bool kWide>
+__device__ __forceinline__ int next_up(uint64_t &w0, uint64_t &w1)
+{
+	if (w0) {
+		const int q = __ffsll((long long)w0) - 1;
+		w0 &= w0 - 1;
+		return q;
+	}
+	if (kWide && w1) {
+		const int q = __ffsll((long long)w1) - 1;
+		w1 &= w1 - 1;
+		return 64 + q;
+	}
+	return -1;
+}
+
+template <bool kWide>
+__device__ __forceinline__ int next_down(uint64_t &w0, uint64_t &w1)
+{
+	if (kWide && w1) {
+		const int q = 63 - __clzll((long long)w1);
+		w1 ^= 1ull << q;
+		return 64 + q;
+	}
+	if (w0) {
+		const int q = 63 - __clzll((long long)w0);
+		w0 ^= 1ull << q;
+		return q;
+	}
+	return -1;
+}
 
 // Pair p's forward and backward max-plus passes over its Johnson order,
-// restricted to the free jobs: X[slot][j] = C of (suffix after j) x
-// (prefix before j), and PI[slot] = (m1 (n+1) | m2 (n+1) << 16, A, B, p):
-// the row offsets of the pair's machines in pt, V and W.
+// restricted to the father's u free jobs `fj`: X[slot][j] = C of (suffix
+// after j) x (prefix before j), and PI[slot] = (m1 (n+1) | m2 (n+1) << 16,
+// A, B, p): the row offsets of the pair's machines in pt, V and W. The
+// free positions come from the job-position table (u lookups, not a scan
+// of all n positions), so both passes touch only the u free entries.
 template <bool kWide>
-__device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restrict__ tjT, int p,
-                                          int slot, int n, int P, int xs, uint32_t w0,
-                                          uint32_t w1, uint32_t w2, uint32_t w3)
+__device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restrict__ tjT,
+                                          const uint8_t *__restrict__ jobposT, int p, int slot,
+                                          int n, int P, int xs, const int16_t *fj, int u)
 {
+	uint64_t m0 = 0, m1 = 0;
+	for (int i = 0; i < u; ++i) {
+		const int q = __ldg(jobposT + (size_t)fj[i] * P + p);
+		if (kWide && q >= 64)
+			m1 |= 1ull << (q - 64);
+		else
+			m0 |= 1ull << q;
+	}
 	const uint2 *e = tjT + p;
 	int32_t *xrow = S.X + slot * xs;
 	int32_t a_sum = 0, b_sum = 0, c = kNeg;
-	for (int q0 = 0; q0 < n; q0 += kWalkBatch) {
+	uint64_t w0 = m0, w1 = m1;
+	for (int left = u; left > 0; left -= kWalkBatch) {
+		int q[kWalkBatch];
 		uint2 v[kWalkBatch];
 #pragma unroll
 		for (int k = 0; k < kWalkBatch; ++k)
-			v[k] = q0 + k < n ? __ldg(e + (size_t)(q0 + k) * P) : make_uint2(0u, 0u);
+			q[k] = next_up<kWide>(w0, w1);
+#pragma unroll
+		for (int k = 0; k < kWalkBatch; ++k)
+			v[k] = q[k] >= 0 ? __ldg(e + (size_t)q[k] * P) : make_uint2(0u, 0u);
 #pragma unroll
 		for (int k = 0; k < kWalkBatch; ++k) {
-			const int job = int(v[k].x & 0xffu);
-			if (q0 + k < n && free_bit<kWide>(w0, w1, w2, w3, job)) {
+			if (q[k] >= 0) {
+				const int job = int(v[k].x & 0xffu);
 				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
 				const int32_t cj = int32_t(v[k].y >> 16); // a + lag + b
 				xrow[job] = c; // C of the prefix before job
@@ -248,15 +285,21 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
 	const int pr = S.pairs[p], ld = n + 1;
 	S.PI[slot] = make_int4((pr & 0xff) * ld | ((pr >> 8) * ld) << 16, a_sum, b_sum, p);
 	int32_t as = 0, bs = 0, cs = kNeg;
-	for (int q0 = n - 1; q0 >= 0; q0 -= kWalkBatch) {
+	w0 = m0;
+	w1 = m1;
+	for (int left = u; left > 0; left -= kWalkBatch) {
+		int q[kWalkBatch];
 		uint2 v[kWalkBatch];
 #pragma unroll
 		for (int k = 0; k < kWalkBatch; ++k)
-			v[k] = q0 - k >= 0 ? __ldg(e + (size_t)(q0 - k) * P) : make_uint2(0u, 0u);
+			q[k] = next_down<kWide>(w0, w1);
+#pragma unroll
+		for (int k = 0; k < kWalkBatch; ++k)
+			v[k] = q[k] >= 0 ? __ldg(e + (size_t)q[k] * P) : make_uint2(0u, 0u);
 #pragma unroll
 		for (int k = 0; k < kWalkBatch; ++k) {
-			const int job = int(v[k].x & 0xffu);
-			if (q0 - k >= 0 && free_bit<kWide>(w0, w1, w2, w3, job)) {
+			if (q[k] >= 0) {
+				const int job = int(v[k].x & 0xffu);
 				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
 				const int32_t cj = int32_t(v[k].y >> 16);
 				const int32_t apre = a_sum - as - a;
@@ -318,6 +361,7 @@ __device__ __forceinline__ int32_t child_pairs(const FamSmem &S, int lo, int hi,
 template <bool kLearned, bool kWide>
 __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, BoundParams bp,
                                                              const uint2 *__restrict__ tjT,
+                                                             const uint8_t *__restrict__ jobposT,
                                                              FamLayout L)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
@@ -348,8 +392,6 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 		// never an access outside the tables
 		for (int i = tid; i < n + 2; i += kFamThreads)
 			S.fr[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
-		if (tid < 4)
-			S.mask[tid] = 0;
 		if (tid == 4)
 			*S.cnt = 0;
 		__syncthreads();
@@ -380,10 +422,7 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 			__syncthreads();
 			continue;
 		}
-		if (tid < u)
-			atomicOr(&S.mask[S.fr[l1 + 1 + tid] >> 5], 1u << (S.fr[l1 + 1 + tid] & 31));
-		__syncthreads();
-		const uint32_t w0 = S.mask[0], w1 = S.mask[1], w2 = S.mask[2], w3 = S.mask[3];
+		const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
 		// first chunk: the K ranked pairs (learned) or pairs [0, pc); its
 		// walks overlap the fronts and backs
 		const int len0 = kLearned ? K : min(L.pc, P);
@@ -394,7 +433,7 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 				int p = t;
 				if (kLearned)
 					p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
-				walk_pair<kWide>(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
+				walk_pair<kWide>(S, tjT, jobposT, p, t, n, P, xs, fj, u);
 			}
 		}
 		// per job: one thread per (job, slice of the chunk's pairs) takes
@@ -412,7 +451,7 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 				const int len = min(L.pc, P - p_lo);
 				__syncthreads(); // previous chunk consumed
 				for (int t = tid; t < len; t += kFamThreads)
-					walk_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+					walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
 				__syncthreads();
 				if (active)
 					job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, xs, accB, accE);
@@ -466,7 +505,7 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 					const int len = min(L.pc, P - p_lo);
 					__syncthreads();
 					for (int t = tid; t < len; t += kFamThreads)
-						walk_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+						walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
 					__syncthreads();
 					if (act2)
 						acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, xs,
@@ -494,7 +533,7 @@ size_t family_smem(const BoundParams &bp, int smem_kb)
 	return fam_layout(bp.n, bp.m, bp.P, size_t(smem_kb > 0 ? smem_kb : 56) * 1024).bytes;
 }
 
-cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, const FamilyArgs &A,
+cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, const FamilyArgs &A,
                               long long max_fathers, int num_sms, cudaStream_t s, int smem_kb)
 {
 	if (max_fathers <= 0)
@@ -513,7 +552,7 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, cons
 	if (e != cudaSuccess)
 		return e;
 	const long long grid = std::min<long long>(max_fathers, (long long)num_sms * std::max(occ, 1));
-	kern<<<unsigned(grid), kFamThreads, L.bytes, s>>>(A, bp, johnsonT, L);
+	kern<<<unsigned(grid), kFamThreads, L.bytes, s>>>(A, bp, T.johnsonT, T.jobposT, L);
 	return cudaGetLastError();
 }
 
@@ -538,7 +577,7 @@ extern "C" int wsbb_decompose_lb2(wsbb_ctx *ctx, const void *fathers, int64_t co
 	A.child_job = child_job;
 	A.stride = ctx->bp.stride;
 	if (e == cudaSuccess)
-		e = wsbb::launch_family_lb2(ctx->bp, ctx->tables.johnsonT, A, count, ctx->num_sms,
+		e = wsbb::launch_family_lb2(ctx->bp, ctx->tables, A, count, ctx->num_sms,
 		                            static_cast<cudaStream_t>(stream));
 	if (e != cudaSuccess)
 		return wsbb_set_error(ctx, WSBB_ERR_CUDA,

@@ -240,6 +240,11 @@ HostTables pack_tables(const Instance &I, std::string &err)
 			dst[2 * e + 1] = p2 | (c << 16);
 		}
 	}
+	// job positions in each pair's Johnson order, job-major: pos[j * P + i]
+	H.imgPos.resize(size_t(I.P) * n);
+	for (int i = 0; i < I.P; ++i)
+		for (int q = 0; q < n; ++q)
+			H.imgPos[size_t(I.johnson[size_t(i) * n + q]) * I.P + i] = uint8_t(q);
 	if (H.t8.bytes > 200 * 1024)
 		err = "bound tables exceed the shared-memory budget (n * m too large)";
 	return H;

@@ -53,11 +53,13 @@ struct DeviceTables {
 	// i, so that threads walking consecutive pairs read consecutive entries
 	// (family bounds): x = job | p1 << 16, y = p2 | (p1 + lag + p2) << 16.
 	const uint2 *johnsonT = nullptr;
+	// jobposT[j * P + i] = position of job j in pair i's Johnson order
+	const uint8_t *jobposT = nullptr;
 };
 
 // Host images of the tables; offsets are relative to each image.
 struct HostTables {
-	std::vector<uint8_t> img8, img16, imgT;
+	std::vector<uint8_t> img8, img16, imgT, imgPos;
 	TableView t8, t16;
 };
 HostTables pack_tables(const Instance &inst, std::string &err);
@@ -105,7 +107,7 @@ struct FamilyArgs {
 };
 // smem_kb: shared-memory budget per CTA in KB (0: 56), which sets the
 // pair-chunk length and how many CTAs share an SM.
-cudaError_t launch_family_lb2(const BoundParams &bp, const uint2 *johnsonT, const FamilyArgs &A,
+cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, const FamilyArgs &A,
                               long long max_fathers, int num_sms, cudaStream_t s,
                               int smem_kb = 0);
 size_t family_smem(const BoundParams &bp, int smem_kb = 0);
