@@ -104,6 +104,7 @@ struct FamSmem {
 	int2 *PF, *PR;
 	int4 *PI;
 	int16_t *fr, *list;
+	uint32_t *mask; // [4] free jobs (scan walks)
 	int *cnt;       // [1]
 };
 
@@ -123,6 +124,7 @@ __device__ __forceinline__ FamSmem carve(uint8_t *smem, const FamLayout &L)
 	S.G = reinterpret_cast<int32_t *>(smem + L.off_G);
 	S.fr = reinterpret_cast<int16_t *>(smem + L.off_fr);
 	S.list = reinterpret_cast<int16_t *>(smem + L.off_list);
+	S.mask = reinterpret_cast<uint32_t *>(smem + L.off_misc);
 	S.cnt = reinterpret_cast<int *>(smem + L.off_misc + 16);
 	return S;
 }
@@ -237,6 +239,72 @@ __device__ __forceinline__ int next_down(uint64_t &w0, uint64_t &w1)
 	return -1;
 }
 
+template <bool kWide>
+__device__ __forceinline__ bool free_bit(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
+                                         int job)
+{
+	const uint32_t lo = (job & 32) ? w1 : w0;
+	if (!kWide) // n <= 64
+		return ((lo >> (job & 31)) & 1u) != 0;
+	const uint32_t hi = (job & 32) ? w3 : w2;
+	return ((((job & 64) ? hi : lo) >> (job & 31)) & 1u) != 0;
+}
+
+constexpr int kScanBatch = 8;
+
+// The same passes as walk_pair below, scanning all n positions of the
+// order and skipping the fixed jobs (free-job mask w0..w3): cheaper than
+// the position-table walk when almost every job is free.
+template <bool kWide>
+__device__ __forceinline__ void scan_pair(const FamSmem &S, const uint2 *__restrict__ tjT, int p,
+                                          int slot, int n, int P, int xs, uint32_t w0,
+                                          uint32_t w1, uint32_t w2, uint32_t w3)
+{
+	const uint2 *e = tjT + p;
+	int32_t *xrow = S.X + slot * xs;
+	int32_t a_sum = 0, b_sum = 0, c = kNeg;
+	for (int q0 = 0; q0 < n; q0 += kScanBatch) {
+		uint2 v[kScanBatch];
+#pragma unroll
+		for (int k = 0; k < kScanBatch; ++k)
+			v[k] = q0 + k < n ? __ldg(e + (size_t)(q0 + k) * P) : make_uint2(0u, 0u);
+#pragma unroll
+		for (int k = 0; k < kScanBatch; ++k) {
+			const int job = int(v[k].x & 0xffu);
+			if (q0 + k < n && free_bit<kWide>(w0, w1, w2, w3, job)) {
+				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
+				const int32_t cj = int32_t(v[k].y >> 16);
+				xrow[job] = c;
+				c = max(c + b, a_sum + cj);
+				a_sum += a;
+				b_sum += b;
+			}
+		}
+	}
+	const int pr = S.pairs[p], ld = n + 1;
+	S.PI[slot] = make_int4((pr & 0xff) * ld | ((pr >> 8) * ld) << 16, a_sum, b_sum, p);
+	int32_t as = 0, bs = 0, cs = kNeg;
+	for (int q0 = n - 1; q0 >= 0; q0 -= kScanBatch) {
+		uint2 v[kScanBatch];
+#pragma unroll
+		for (int k = 0; k < kScanBatch; ++k)
+			v[k] = q0 - k >= 0 ? __ldg(e + (size_t)(q0 - k) * P) : make_uint2(0u, 0u);
+#pragma unroll
+		for (int k = 0; k < kScanBatch; ++k) {
+			const int job = int(v[k].x & 0xffu);
+			if (q0 - k >= 0 && free_bit<kWide>(w0, w1, w2, w3, job)) {
+				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
+				const int32_t cj = int32_t(v[k].y >> 16);
+				const int32_t apre = a_sum - as - a;
+				xrow[job] = max(xrow[job] + bs, apre + cs);
+				cs = max(cs + a, bs + cj);
+				as += a;
+				bs += b;
+			}
+		}
+	}
+}
+
 // Pair p's forward and backward max-plus passes over its Johnson order,
 // restricted to the father's u free jobs `fj`: X[slot][j] = C of (suffix
 // after j) x (prefix before j), and PI[slot] = (m1 (n+1) | m2 (n+1) << 16,
@@ -249,12 +317,16 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
                                           int n, int P, int xs, const int16_t *fj, int u)
 {
 	uint64_t m0 = 0, m1 = 0;
+#pragma unroll 8
 	for (int i = 0; i < u; ++i) {
 		const int q = __ldg(jobposT + (size_t)fj[i] * P + p);
-		if (kWide && q >= 64)
-			m1 |= 1ull << (q - 64);
-		else
+		if (kWide) {
+			const uint64_t bit = 1ull << (q & 63);
+			m0 |= q < 64 ? bit : 0ull;
+			m1 |= q < 64 ? 0ull : bit;
+		} else {
 			m0 |= 1ull << q;
+		}
 	}
 	const uint2 *e = tjT + p;
 	int32_t *xrow = S.X + slot * xs;
@@ -423,6 +495,18 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 			continue;
 		}
 		const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
+		// walks: scan all n positions when more than 3/4 of the jobs are
+		// free, else follow the position table over the free ones only
+		const bool scan = 4 * u > 3 * n;
+		if (scan) {
+			if (tid < 4)
+				S.mask[tid] = 0;
+			__syncthreads();
+			if (tid < u)
+				atomicOr(&S.mask[fj[tid] >> 5], 1u << (fj[tid] & 31));
+			__syncthreads();
+		}
+		const uint32_t w0 = S.mask[0], w1 = S.mask[1], w2 = S.mask[2], w3 = S.mask[3];
 		// first chunk: the K ranked pairs (learned) or pairs [0, pc); its
 		// walks overlap the fronts and backs
 		const int len0 = kLearned ? K : min(L.pc, P);
@@ -433,7 +517,10 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 				int p = t;
 				if (kLearned)
 					p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
-				walk_pair<kWide>(S, tjT, jobposT, p, t, n, P, xs, fj, u);
+				if (scan)
+					scan_pair<kWide>(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
+				else
+					walk_pair<kWide>(S, tjT, jobposT, p, t, n, P, xs, fj, u);
 			}
 		}
 		// per job: one thread per (job, slice of the chunk's pairs) takes
@@ -451,7 +538,12 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 				const int len = min(L.pc, P - p_lo);
 				__syncthreads(); // previous chunk consumed
 				for (int t = tid; t < len; t += kFamThreads)
-					walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+					{
+					if (scan)
+						scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+					else
+						walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+				}
 				__syncthreads();
 				if (active)
 					job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, xs, accB, accE);
@@ -505,7 +597,12 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 					const int len = min(L.pc, P - p_lo);
 					__syncthreads();
 					for (int t = tid; t < len; t += kFamThreads)
+						{
+					if (scan)
+						scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+					else
 						walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+				}
 					__syncthreads();
 					if (act2)
 						acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, xs,
