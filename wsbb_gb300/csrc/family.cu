@@ -144,11 +144,15 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 	if (warp == 0) {
 		int32_t Fk = 0;
 		const int nj = l1 + 1;
+		// the time added at step s is loaded one step ahead, off the chain
+		int32_t add = (lane < m && lane == 0 && nj > 0) ? S.pt[S.fr[0]] : 0;
 		for (int s = 0; s < nj + m - 1; ++s) {
+			const int i = s - lane, i1 = i + 1;
+			const int32_t next = (lane < m && i1 >= 0 && i1 < nj) ? S.pt[lane * ld + S.fr[i1]] : 0;
 			const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
-			const int i = s - lane;
 			if (lane < m && i >= 0 && i < nj)
-				Fk = max(Fk, lane > 0 ? left : 0) + S.pt[lane * ld + S.fr[i]];
+				Fk = max(Fk, lane > 0 ? left : 0) + add;
+			add = next;
 		}
 		if (lane < m) {
 			S.F[lane] = Fk;
@@ -172,11 +176,15 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 	} else if (warp == 1) {
 		int32_t Gq = 0;
 		const int nj = n - l2;
+		int32_t add = (lane < m && lane == 0 && nj > 0) ? S.pt[(m - 1) * ld + S.fr[n - 1]] : 0;
 		for (int s = 0; s < nj + m - 1; ++s) {
+			const int i = s - lane, i1 = i + 1;
+			const int32_t next =
+			    (lane < m && i1 >= 0 && i1 < nj) ? S.pt[(m - 1 - lane) * ld + S.fr[n - 1 - i1]] : 0;
 			const int32_t left = __shfl_up_sync(0xffffffffu, Gq, 1);
-			const int i = s - lane;
 			if (lane < m && i >= 0 && i < nj)
-				Gq = max(Gq, lane > 0 ? left : 0) + S.pt[(m - 1 - lane) * ld + S.fr[n - 1 - i]];
+				Gq = max(Gq, lane > 0 ? left : 0) + add;
+			add = next;
 		}
 		if (lane < m)
 			S.G[lane] = Gq;
@@ -495,9 +503,10 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 			continue;
 		}
 		const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
-		// walks: scan all n positions when more than 3/4 of the jobs are
-		// free, else follow the position table over the free ones only
-		const bool scan = 4 * u > 3 * n;
+		// walks: scan all n positions when most jobs are free (more than
+		// 3/4, or half for n > 64 where the position masks take two
+		// words), else follow the position table over the free ones only
+		const bool scan = kWide ? 2 * u > n : 4 * u > 3 * n;
 		if (scan) {
 			if (tid < 4)
 				S.mask[tid] = 0;
