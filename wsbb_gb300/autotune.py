@@ -20,7 +20,7 @@ import json
 import os
 import sys
 
-WINDOWS = (2048, 4096, 8192, 16384, 32768)
+WINDOWS = (512, 1024, 2048, 4096, 8192, 16384, 32768)
 SMEM_KB = (56, 100, 160)
 
 

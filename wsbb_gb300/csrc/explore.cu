@@ -99,6 +99,10 @@ struct ExDev {
 	long long iterations;
 	int ub, best, done, error;
 	int win, win_min, win_max, doom;
+	// growth ceiling of the window: window / 16 after an incumbent
+	// improvement, doubling every 128 iterations without one (speculation
+	// against a stale incumbent is what an improvement discards)
+	int win_cap, calm;
 	unsigned long long branched, pruned, leaves, improved, bounded;
 	unsigned long long evaluated, discarded, scanned, committed;
 	unsigned long long early;      // children settled by the learned K-pair test
@@ -379,7 +383,15 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 		D->ub = ub;
 		D->top = top;
 		D->doom = ub < ub0 ? 1 : 0;
-		D->win = ub < ub0 ? D->win_min : min(D->win_max, 2 * D->win);
+		if (ub < ub0) {
+			D->win = D->win_min;
+			D->win_cap = max(D->win_min, D->win_max >> 4);
+			D->calm = 0;
+		} else {
+			if ((++D->calm & 127) == 0)
+				D->win_cap = min(D->win_max, 2 * D->win_cap);
+			D->win = min(D->win_cap, 2 * D->win);
+		}
 		D->iterations += 1;
 		D->region_len = 0;
 		D->region_slots = 0;
@@ -832,6 +844,8 @@ __global__ void init_kernel(ExParams P, int ub0, int best, int win_min, int win_
 		D->win = win_min;
 		D->win_min = win_min;
 		D->win_max = win_max;
+		D->win_cap = win_max;
+		D->calm = 0;
 		Meta m0 = {0, 0, ST_UNPROC, 0};
 		P.meta[0] = m0;
 	}
@@ -1234,7 +1248,9 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 }
 
 // Window bounds: at most `window` fathers per iteration, shrinking to
-// window / 64 (at least 64) after an incumbent improvement.
+// window / 64 (at least 64) after an incumbent improvement, then doubling
+// per iteration up to a ceiling that is window / 16 right after the
+// improvement and doubles every 128 iterations without one.
 int window_min_of(int window) { return std::min(window, std::max(64, window / 64)); }
 
 void fill_stats(const wsbb::ExDev &h, const int16_t *best_rec, int n, int status,

@@ -25,22 +25,30 @@ TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost",
 
 def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: str = "default",
         device: int = 0, verbose: bool = True, model_path: str = "", Ks=(8,),
-        per_child: bool = False, capacity: int = 0) -> dict:
+        per_child: bool = False, capacity: int = 0, tune: bool = False) -> dict:
     """`per_child` also runs the search with every child bounded on its own
-    (the per-node LB2 kernel) and reports its time and tree check."""
+    (the per-node LB2 kernel) and reports its time and tree check. `tune`
+    takes the window and family tile from the autotuner (tuned on the first
+    instance, cached per GPU and shape) instead of `window`."""
     model = None
     if model_path:
         from .learned import Model
         model = Model(n, m)
         model.load(model_path)
     runs = []
+    kb = 0
+    shape = None
     for s in seeds:
         p = gen_instance(s, n, m)
         ub0, _ = neh(p)
         ctx = Context(p, device=device)
         best = 99999 if best_mode == "default" else ub0
+        if tune and shape is None:
+            from .autotune import tuned
+            shape = tuned(ctx, ub0, best, device=device)
+            window, kb = shape["window"], shape["family_smem_kb"]
         r = explore(ctx, ub0=ub0, best=best, window=window, max_iters=max_iters,
-                    capacity=capacity)
+                    capacity=capacity, family_smem_kb=kb)
         row = {"n": n, "m": m, "seed": s, "neh": ub0, "best": best,
                "optimum": r["best_cost"], "proved": r["status"] == 0,
                "branched": r["branched"], "pruned": r["pruned"], "leaves": r["leaves"],
@@ -83,7 +91,7 @@ def run(n: int, m: int, seeds, window: int = 0, max_iters: int = 0, best_mode: s
             print(json.dumps(row), flush=True)
     tot_b = sum(r["bounded"] for r in runs)
     tot_s = sum(r["seconds"] for r in runs)
-    out = {"runs": runs, "bounded": tot_b, "seconds": tot_s,
+    out = {"runs": runs, "bounded": tot_b, "seconds": tot_s, "shape": shape,
            "bounded_per_s": tot_b / max(tot_s, 1e-12),
            "evaluated": sum(r["evaluated"] for r in runs),
            "all_proved": all(r["proved"] for r in runs)}
@@ -124,9 +132,11 @@ def main(argv=None) -> None:
                     help="also search with per-child LB2 (the per-node kernel)")
     ap.add_argument("--capacity", type=int, default=0,
                     help="stack capacity in nodes (0: the library's default)")
+    ap.add_argument("--tune", action="store_true",
+                    help="window and family tile from the autotuner")
     a = ap.parse_args(argv)
     out = run(a.n, a.m, a.seeds, a.window, a.max_iters, a.best, model_path=a.model, Ks=a.K,
-              per_child=a.per_child, capacity=a.capacity)
+              per_child=a.per_child, capacity=a.capacity, tune=a.tune)
     summary = {k: v for k, v in out.items() if k != "runs"}
     print(json.dumps({"summary": summary}), flush=True)
 
