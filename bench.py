@@ -4,10 +4,11 @@ per-child, learned and CPU arms on the same tree.
 Workload (one step = one search): permutation flowshop n = 50 jobs, m = 20
 machines (190 machine pairs), processing times uniform in [1, 99] from seed
 0; begin-end branching from the NEH incumbent with side-choice threshold
-best = NEH (the learned-selector configuration), 400 batched iterations
-with the window and family-bounds tile the autotuner picks for this GPU
-(wsbb_gb300.autotune, untimed). Every step explores the same tree prefix
-(its counters are checked against the first step's). The search state grows to
+best = NEH (the learned-selector configuration); a step explores the first
+250 M nodes of the tree (a node budget: the search commits in DFS order, so
+that is the same tree prefix whatever the window), with the window and
+family-bounds tile the autotuner picks for this GPU (wsbb_gb300.autotune,
+untimed). Every step's counters are checked against the first step's. The search state grows to
 gigabytes over a step, far beyond the 129 MB L2; L2 is also flushed between
 steps.
 
@@ -51,7 +52,9 @@ sys.path.insert(0, ROOT)
 METRIC = ("bounded nodes/sec & time-to-proof (learned+batched vs plain GPU LB2 vs CPU), "
           "same tree")
 UNIT = "bounded nodes/s"
-S_N, S_M, S_ITERS = 50, 20, 400
+# one step: the first S_NODES tree nodes of the search (the search commits
+# in DFS order, so that is the same tree prefix whatever the window)
+S_N, S_M, S_NODES, S_ITER_CAP = 50, 20, 250_000_000, 20_000
 MODEL = os.path.join(ROOT, "wsbb_gb300", "models", f"selector_n{S_N}_m{S_M}.npz")
 TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost", "coverage")
 # kernels per search iteration (family bounds): commit, doom, select x3,
@@ -64,9 +67,9 @@ PROOF_N, PROOF_M, PROOF_SEEDS = 50, 10, (0, 1, 2, 3, 4)
 
 def workload_config(seed: int, extra: dict | None = None) -> dict:
     cfg = {"workload": f"exact begin-end DFS, n={S_N} jobs m={S_M} machines (190 pairs), "
-                       f"seed {seed}, NEH incumbent, best=NEH, {S_ITERS} batched iterations "
-                       "per step (autotuned window and tile)",
-           "n": S_N, "m": S_M, "seed": seed, "iterations_per_step": S_ITERS,
+                       f"seed {seed}, NEH incumbent, best=NEH, the first {S_NODES // 10**6} M tree "
+                       "nodes per step (autotuned window and tile)",
+           "n": S_N, "m": S_M, "seed": seed, "tree_nodes_per_step": S_NODES,
            "l2": "search state >> L2 (GBs), L2 flushed between steps"}
     if extra:
         cfg.update(extra)
@@ -364,11 +367,12 @@ def run_gpu(args) -> None:
     # launch shapes (window, family-bounds tile) from the autotuner: a short
     # prefix of this search per candidate, untimed
     from wsbb_gb300 import autotune
-    shape = autotune.tuned(ctx, ub0, ub0, device=local)
+    shape = autotune.tuned(ctx, ub0, ub0, device=local, node_budget=S_NODES)
     win, kb = shape["window"], shape["family_smem_kb"]
 
     def step():
-        return explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr, window=win,
+        return explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITER_CAP, max_bounded=S_NODES,
+                       stream=sptr, window=win,
                        family_smem_kb=kb)
 
     ref = None
@@ -406,7 +410,7 @@ def run_gpu(args) -> None:
     L = W.lib()
     h_p = np.ascontiguousarray(p, dtype=np.int32)
     from wsbb_gb300.explorer import ExploreCfg, ExploreStats
-    cfg = ExploreCfg(ub0, ub0, win, 0, 0, S_ITERS, 0, kb)
+    cfg = ExploreCfg(ub0, ub0, win, 0, 0, S_ITER_CAP, 0, kb, S_NODES)
     e2e_steps = max(2, min(args.steps, 5))
     h2d = d2h = 0
     e2e_bounded = 0
@@ -434,14 +438,16 @@ def run_gpu(args) -> None:
                     "same_tree": all(r[k] == ref[k] for k in TREE_KEYS),
                     "speedup_vs_per_child_lb2": base_s / r["seconds"]}
         fam = step()
-        per = explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITERS, stream=sptr, child_lb2=True,
+        per = explore(ctx, ub0=ub0, best=ub0, max_iters=S_ITER_CAP, max_bounded=S_NODES,
+                      stream=sptr, child_lb2=True,
                       window=win)
         arms = {"per_child_lb2": arm(per, per["seconds"]), "family_lb2": arm(fam, per["seconds"])}
         if os.path.exists(MODEL):
             model = Model(S_N, S_M)
             model.load(MODEL)
             for K, pc in ((16, True), (4, False)):
-                q = explore_learned(ctx, model, K, ub0=ub0, best=ub0, max_iters=S_ITERS,
+                q = explore_learned(ctx, model, K, ub0=ub0, best=ub0, max_iters=S_ITER_CAP,
+                                    max_bounded=S_NODES,
                                     stream=sptr, child_lb2=pc, window=win)
                 a = arm(q, per["seconds"])
                 a["early_share"] = q["early"] / max(1, q["evaluated"])

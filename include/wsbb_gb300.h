@@ -162,6 +162,10 @@ typedef struct {
 	                           0: 56): the pair-chunk length, and with it how
 	                           many CTAs share an SM (a tile shape the
 	                           autotuner picks) */
+	int64_t max_bounded; /* stop once this many tree nodes are bounded,
+	                        checked between graph launches (0: no limit);
+	                        the search commits in DFS order, so a budget is
+	                        the same tree prefix whatever the window */
 } wsbb_explore_cfg;
 
 typedef struct {

@@ -125,3 +125,19 @@ def test_concurrent_searches_on_many_contexts():
         a = out["arms"][arm]
         assert a["instances"] == 9 and a["same_tree"], arm
     assert out["arms"]["family"]["bounded"] == out["arms"]["per_child"]["bounded"] > 0
+
+
+def test_node_budget_stops_the_search():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import wsbb_gb300 as W
+    from wsbb_gb300.explorer import explore
+    p = W.gen_instance(1, 20, 20)
+    ub, _ = W.neh(p)
+    ctx = W.Context(p)
+    full = explore(ctx, ub0=ub)
+    budget = full["bounded"] // 10
+    for window in (1024, 8192):
+        r = explore(ctx, ub0=ub, window=window, max_bounded=budget)
+        assert r["status"] == 1 and budget <= r["bounded"] < full["bounded"]

@@ -6,10 +6,13 @@ Two shapes set how the batched search maps onto the GPU:
   family_smem_kb  shared memory per CTA of the family bounds: how many
                   machine pairs one chunk holds (their per-job X rows) and
                   with it how many CTAs share an SM
-Neither changes the tree. `tune` times a short prefix of the search for
-every candidate pair and keeps the one with the most bounded nodes per
-second; `tuned` caches the choice per (GPU, n, m, best mode) in
-~/.cache/wsbb_gb300/autotune.json (WSBB_GB300_CACHE overrides the folder).
+Neither changes the tree. `tune` times the same prefix of the search for
+every candidate pair — the first `node_budget` tree nodes (the search
+commits in DFS order, so a node budget is the same tree prefix whatever the
+window; an iteration count is not) — and keeps the one with the most
+bounded nodes per second; `tuned` caches the choice per (GPU, n, m, best
+mode) in ~/.cache/wsbb_gb300/autotune.json (WSBB_GB300_CACHE overrides the
+folder).
 
     python -m wsbb_gb300.autotune --n 50 --m 20 --best ub0
 """
@@ -21,7 +24,7 @@ import os
 import sys
 
 WINDOWS = (512, 1024, 2048, 4096, 8192, 16384, 32768)
-SMEM_KB = (56, 100, 160)
+SMEM_KB = (56, 100)
 
 
 def cache_path() -> str:
@@ -30,8 +33,10 @@ def cache_path() -> str:
     return os.path.join(root, "autotune.json")
 
 
-def cache_key(device_name: str, n: int, m: int, best_is_ub: bool) -> str:
-    return f"{device_name}|n={n}|m={m}|best={'ub0' if best_is_ub else 'default'}"
+def cache_key(device_name: str, n: int, m: int, best_is_ub: bool,
+              node_budget: int = 50_000_000) -> str:
+    return (f"{device_name}|n={n}|m={m}|best={'ub0' if best_is_ub else 'default'}"
+            f"|budget={node_budget}")
 
 
 def load_cache(path: str | None = None) -> dict:
@@ -63,14 +68,15 @@ def pick(results: list[dict], tolerance: float = 0.01) -> dict:
     return min(near, key=lambda r: (r["family_smem_kb"], r["window"]))
 
 
-def tune(ctx, ub0: int, best: int, iters: int = 96, windows=WINDOWS, smem_kbs=SMEM_KB,
-         capacity: int = 0, stream: int = 0) -> tuple[dict, list[dict]]:
+def tune(ctx, ub0: int, best: int, node_budget: int = 50_000_000, iters: int = 4000,
+         windows=WINDOWS, smem_kbs=SMEM_KB, capacity: int = 0,
+         stream: int = 0) -> tuple[dict, list[dict]]:
     from .explorer import explore
     results = []
     for w in windows:
         for kb in smem_kbs:
             r = explore(ctx, ub0=ub0, best=best, window=w, max_iters=iters, capacity=capacity,
-                        family_smem_kb=kb, stream=stream)
+                        family_smem_kb=kb, stream=stream, max_bounded=node_budget)
             results.append({"window": w, "family_smem_kb": kb, "iterations": r["iterations"],
                             "bounded": r["bounded"], "seconds": r["seconds"],
                             "bounded_per_s": r["bounded"] / max(r["seconds"], 1e-12)})
@@ -81,7 +87,7 @@ def tuned(ctx, ub0: int, best: int, device: int = 0, retune: bool = False, **kw)
     """The cached choice for this GPU and instance shape, tuning on a miss."""
     import torch
     name = torch.cuda.get_device_name(device)
-    key = cache_key(name, ctx.n, ctx.m, best == ub0)
+    key = cache_key(name, ctx.n, ctx.m, best == ub0, kw.get("node_budget", 50_000_000))
     if not retune:
         hit = load_cache().get(key)
         if hit:
@@ -98,15 +104,15 @@ def main(argv=None) -> None:
     ap.add_argument("--m", type=int, default=20)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--best", default="ub0", choices=["default", "ub0"])
-    ap.add_argument("--iters", type=int, default=96)
+    ap.add_argument("--budget", type=int, default=50_000_000)
     a = ap.parse_args(argv)
     p = gen_instance(a.seed, a.n, a.m)
     ub0, _ = neh(p)
     ctx = Context(p)
     best = ub0 if a.best == "ub0" else 99999
-    choice, results = tune(ctx, ub0, best, iters=a.iters)
+    choice, results = tune(ctx, ub0, best, node_budget=a.budget)
     import torch
-    store(cache_key(torch.cuda.get_device_name(0), a.n, a.m, a.best == "ub0"), choice)
+    store(cache_key(torch.cuda.get_device_name(0), a.n, a.m, a.best == "ub0", a.budget), choice)
     print(json.dumps({"choice": choice, "candidates": results}), flush=True)
 
 

@@ -1440,7 +1440,8 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 			e = cudaStreamSynchronize(s);
 		if (e != cudaSuccess || h.done || h.error)
 			break;
-		if (launched >= max_iters || (M.mode == 2 && (long long)h.log_count >= M.log_cap)) {
+		if (launched >= max_iters || (M.mode == 2 && (long long)h.log_count >= M.log_cap) ||
+		    (cfg->max_bounded > 0 && (long long)h.bounded >= cfg->max_bounded)) {
 			status = 1; // iteration cap, or the training-record buffer is full
 			break;
 		}
@@ -1611,7 +1612,8 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 			e = cudaStreamSynchronize(s);
 		if (e != cudaSuccess || h.done || h.error)
 			break;
-		if (launched >= max_iters) {
+		if (launched >= max_iters ||
+		    (cfg->max_bounded > 0 && (long long)h.bounded >= cfg->max_bounded)) {
 			status = 1;
 			break;
 		}

@@ -22,7 +22,8 @@ MAX_JOBS = 128
 class ExploreCfg(C.Structure):
     _fields_ = [("ub0", C.c_int32), ("best", C.c_int32), ("window", C.c_int32),
                 ("graph_iters", C.c_int32), ("capacity", C.c_int64), ("max_iters", C.c_int64),
-                ("flags", C.c_int32), ("family_smem_kb", C.c_int32)]
+                ("flags", C.c_int32), ("family_smem_kb", C.c_int32),
+                ("max_bounded", C.c_int64)]
 
 
 class ExploreStats(C.Structure):
@@ -46,7 +47,8 @@ def coverage(hist, n: int) -> int:
 
 def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int = 0,
             graph_iters: int = 0, capacity: int = 0, max_iters: int = 0, graph: bool = True,
-            stream: int = 0, child_lb2: bool = False, family_smem_kb: int = 0) -> dict:
+            stream: int = 0, child_lb2: bool = False, family_smem_kb: int = 0,
+            max_bounded: int = 0) -> dict:
     """The exact GPU search. `child_lb2` bounds each child record on its own
     with the per-node LB2 kernel (the reference GPU kernel's form) instead of
     each father's children together; bounds and tree are the same."""
@@ -55,7 +57,7 @@ def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int
     flags = (0 if graph else NO_GRAPH) | (CHILD_LB2 if child_lb2 else 0)
     cfg = ExploreCfg(INT32_MAX if ub0 is None else int(ub0), int(best), int(window),
                      int(graph_iters), int(capacity), int(max_iters), flags,
-                     int(family_smem_kb))
+                     int(family_smem_kb), int(max_bounded))
     st = ExploreStats()
     rc = L.wsbb_explore(ctx.h, C.byref(cfg), C.byref(st), stream or None)
     if rc != 0:

@@ -133,14 +133,14 @@ def _stats_dict(st: ExploreStats, n: int) -> dict:
 def explore_learned(ctx: Context, model: Model, K: int, ub0: int | None = None,
                     best: int | None = None, window: int = 0, max_iters: int = 0,
                     graph_iters: int = 0, stream: int = 0, child_lb2: bool = False,
-                    capacity: int = 0, family_smem_kb: int = 0) -> dict:
+                    capacity: int = 0, family_smem_kb: int = 0, max_bounded: int = 0) -> dict:
     """The exact search with the learned K-pair test; `best` defaults to ub0.
     `child_lb2`: the test and the full-LB2 fallback per child record (the
     per-node kernels) instead of per father (family bounds)."""
     ub = INT32_MAX if ub0 is None else int(ub0)
     cfg = ExploreCfg(ub, int(ub if best is None else best), int(window), int(graph_iters),
                      int(capacity), int(max_iters), CHILD_LB2 if child_lb2 else 0,
-                     int(family_smem_kb))
+                     int(family_smem_kb), int(max_bounded))
     st = ExploreStats()
     rc = _L().wsbb_explore_learned(ctx.h, C.byref(cfg), model.h, int(K), C.byref(st),
                                    stream or None)
