@@ -146,3 +146,14 @@ def test_autotune_cache_and_pick(tmp_path, monkeypatch):
     data = A.load_cache()
     assert data[key] == rs[1] and len(data) == 2
     assert A.cache_path().startswith(str(tmp_path))
+
+
+def test_multi_instance_shapes_and_capacity():
+    from wsbb_gb300 import multi_bench as M
+    shapes = [M.shape_of(i) for i in range(64)]
+    assert shapes[:4] == [(20, 5), (50, 5), (100, 5), (20, 10)]
+    assert len(set(shapes)) == 9
+    assert sum(1 for n, m in shapes if m == 20) == 21
+    assert M.capacity_of(20, 4096, 64) == 1 << 22          # floor
+    assert M.capacity_of(100, 4096, 64) == 13107200
+    assert M.capacity_of(128, 1 << 16, 1 << 10) == 1 << 25  # ceiling
