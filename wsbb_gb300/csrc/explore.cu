@@ -256,8 +256,13 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 			if (idx >= 0 && e[i].state == ST_LEAF)
 				leaf_min = min(leaf_min, e[i].lb);
 		}
-		const int ub_in = min(ub, block_excl_scan<kSelThreads>(leaf_min, MinOp(), INT_MAX, s_int,
-		                                                       (int *)nullptr));
+		// leaves are rare: without one in the chunk the incumbent cannot
+		// change in it, and both leaf scans below are skipped
+		const int any_leaf = __syncthreads_or(leaf_min != INT_MAX);
+		const int ub_in =
+		    any_leaf ? min(ub, block_excl_scan<kSelThreads>(leaf_min, MinOp(), INT_MAX, s_int,
+		                                                    (int *)nullptr))
+		             : ub;
 		// first entry that cannot be committed: an unprocessed node, the
 		// stack bottom, or a marker failing against the running incumbent
 		int first_stop = kChunk;
@@ -320,7 +325,8 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 					atomicAdd(&s_hist[hkey], (unsigned long long)sum);
 			}
 		}
-		const int cmin = block_reduce<kSelThreads>(chunk_min, MinOp(), INT_MAX, s_int);
+		const int cmin =
+		    any_leaf ? block_reduce<kSelThreads>(chunk_min, MinOp(), INT_MAX, s_int) : INT_MAX;
 		if (cmin < ub) {
 			// the first leaf reaching the new minimum is the one that set it
 			const int first = block_reduce<kSelThreads>(chunk_min == cmin ? first_min : kChunk,
