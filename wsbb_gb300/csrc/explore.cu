@@ -318,11 +318,14 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 					}
 				}
 				// one shared atomic per distinct depth per warp: most entries
-				// of a chunk share a few depths
-				const unsigned grp = __match_any_sync(0xffffffffu, hkey);
-				const unsigned sum = __reduce_add_sync(grp, hval);
-				if (hkey != 255 && (threadIdx.x & 31) == __ffs(grp) - 1)
-					atomicAdd(&s_hist[hkey], (unsigned long long)sum);
+				// of a chunk share a few depths (warps with nothing to add,
+				// past the committed run, skip it)
+				if (__any_sync(0xffffffffu, hkey != 255)) {
+					const unsigned grp = __match_any_sync(0xffffffffu, hkey);
+					const unsigned sum = __reduce_add_sync(grp, hval);
+					if (hkey != 255 && (threadIdx.x & 31) == __ffs(grp) - 1)
+						atomicAdd(&s_hist[hkey], (unsigned long long)sum);
+				}
 			}
 		}
 		const int cmin =
