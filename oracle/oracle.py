@@ -233,12 +233,16 @@ class RefBound:
 
 
 def ref_explore(p: np.ndarray, ub0: int | None = None, best: int = 99999,
-                timeout: float = 600.0) -> dict:
-    """Run the reference's CPU search (oracle/_ref/ref_explore) on `p`."""
+                timeout: float = 600.0, workdir: str | None = None) -> dict:
+    """Run the reference's CPU search (oracle/_ref/ref_explore) on `p`.
+    `workdir`: the working directory, where the reference reads its initial
+    incumbents from bab.solutions (with ub0 None, a file already there is
+    kept) and appends every improvement to it; a temporary one if None."""
     m, n = p.shape
-    with tempfile.TemporaryDirectory() as d:
+    with tempfile.TemporaryDirectory() as tmp:
+        d = workdir or tmp
         r = subprocess.run([_REF_EXPLORE, str(n), str(m), str(-1 if ub0 is None else ub0),
-                            str(best), d + "/"],
+                            str(best), d.rstrip("/") + "/"],
                            input=" ".join(str(int(x)) for x in p.ravel()),
                            capture_output=True, text=True, timeout=timeout, check=True)
     line = [ln for ln in r.stdout.splitlines() if ln.startswith("RESULT ")][-1]
