@@ -89,6 +89,8 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 		e = cudaMemcpy(base + H.img8.size() + H.img16.size() + H.imgT.size(), H.imgPos.data(),
 		               H.imgPos.size(), cudaMemcpyHostToDevice);
 	if (e == cudaSuccess)
+		e = cudaMalloc(&ctx->d_claim, sizeof(unsigned long long));
+	if (e == cudaSuccess)
 		e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
 	if (e != cudaSuccess) {
 		fprintf(stderr, "wsbb_ctx_create: %s\n", cudaGetErrorString(e));
@@ -130,6 +132,8 @@ extern "C" void wsbb_ctx_destroy(wsbb_ctx *ctx)
 		cudaFree(ctx->d_recs);
 	if (ctx->d_out)
 		cudaFree(ctx->d_out);
+	if (ctx->d_claim)
+		cudaFree(ctx->d_claim);
 	if (ctx->stream)
 		cudaStreamDestroy(ctx->stream);
 	delete ctx;
@@ -149,8 +153,14 @@ cudaError_t allow_max_dynamic_smem_fn(const void *kernel)
 		return cudaSuccess;
 	int max_optin = 0;
 	e = cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+	// the ceiling covers dynamic shared memory only: the kernel's static
+	// shared memory comes off the device's per-block maximum
+	cudaFuncAttributes fa;
 	if (e == cudaSuccess)
-		e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_optin);
+		e = cudaFuncGetAttributes(&fa, kernel);
+	if (e == cudaSuccess)
+		e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         max_optin - int(fa.sharedSizeBytes));
 	if (e == cudaSuccess)
 		done.insert({dev, kernel});
 	return e;

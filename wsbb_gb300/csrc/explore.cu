@@ -105,6 +105,7 @@ struct ExDev {
 	int win_cap, calm;
 	unsigned long long branched, pruned, leaves, improved, bounded;
 	unsigned long long evaluated, discarded, scanned, committed;
+	unsigned long long fam_next;   // fathers claimed by the family-bounds CTAs
 	unsigned long long early;      // children settled by the learned K-pair test
 	unsigned long long settled_fathers; // fathers whose children it settled all
 	long long n_unsettled;         // children left for full LB2 this iteration
@@ -407,6 +408,7 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 		D->n_fathers = 0;
 		D->n_children = 0;
 		D->n_unsettled = 0;
+		D->fam_next = 0;
 		if (top < 0)
 			D->done = 1;
 	}
@@ -1219,6 +1221,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			fa.child_lb = X.P.child_lb;
 			fa.child_job = X.P.child_job;
 			fa.stride = X.P.stride;
+			fa.next = &X.P.dev->fam_next;
 			fa.fpairs = X.P.fpairs;
 			fa.K = X.P.K;
 			fa.ub_dev = &X.P.dev->ub;
@@ -1243,6 +1246,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 			fa.child_lb = X.P.child_lb;
 			fa.child_job = X.P.child_job;
 			fa.stride = X.P.stride;
+			fa.next = &X.P.dev->fam_next;
 			e = launch_family_lb2(ctx->bp, ctx->tables, fa, X.window, ctx->num_sms, s,
 			                      X.fam_kb);
 		}

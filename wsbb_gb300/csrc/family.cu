@@ -465,169 +465,183 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 	const int thr = kLearned ? max(*A.best_dev, *A.ub_dev) : 0;
 	const int K = kLearned ? min(A.K, P) : 0;
 
-	for (long long f = blockIdx.x; f < nf; f += gridDim.x) {
-		const long long ri = A.ridx ? A.ridx[f] : f;
-		const int16_t *g_fr = reinterpret_cast<const int16_t *>(A.fathers + ri * A.stride);
-		// job ids clamped to [0, n): a malformed record gives wrong bounds,
-		// never an access outside the tables
-		for (int i = tid; i < n + 2; i += kFamThreads)
-			S.fr[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
-		if (tid == 4)
-			*S.cnt = 0;
-		__syncthreads();
-		const int l1 = S.fr[n], l2 = S.fr[n + 1];
-		const int u = l2 - l1 - 1;
-		const long long c0 = A.child_off[f];
-		// cursors outside -1 <= l1, l2 <= n with two free jobs or more, or a
-		// child range of another size: the father is skipped
-		if (l1 < -1 || l2 > n || u < 2 || A.child_off[f + 1] - c0 != (u == 2 ? 2 : 2 * u)) {
+	// fathers: the CTA's own first, then the next unclaimed one from the
+	// device counter (A.next, zero at launch), so CTAs that drew light
+	// fathers take more and none idles at the tail; without a counter,
+	// every gridDim.x-th father
+	__shared__ long long s_next;
+	for (long long f = blockIdx.x; f < nf;) {
+		do {
+			const long long ri = A.ridx ? A.ridx[f] : f;
+			const int16_t *g_fr = reinterpret_cast<const int16_t *>(A.fathers + ri * A.stride);
+			// job ids clamped to [0, n): a malformed record gives wrong bounds,
+			// never an access outside the tables
+			for (int i = tid; i < n + 2; i += kFamThreads)
+				S.fr[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
+			if (tid == 4)
+				*S.cnt = 0;
 			__syncthreads();
-			continue;
-		}
-		if (u == 2) {
-			// two leaves: makespans of front + (x, y) + back, both orders
-			fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, true);
-			__syncthreads();
-			if (tid < 2) {
-				const int x = S.fr[l1 + 1 + tid], y = S.fr[l1 + 2 - tid];
-				int32_t v1 = 0, v2 = 0, mk = 0;
-				for (int k = 0; k < m; ++k) {
-					v1 = max(v1, S.F[k]) + S.pt[k * (n + 1) + x];
-					v2 = max(v2, v1) + S.pt[k * (n + 1) + y];
-					mk = max(mk, v2 + S.G[m - 1 - k]);
-				}
-				A.child_lb[c0 + tid] = mk;
-				A.child_job[c0 + tid] = int16_t(x);
+			const int l1 = S.fr[n], l2 = S.fr[n + 1];
+			const int u = l2 - l1 - 1;
+			const long long c0 = A.child_off[f];
+			// cursors outside -1 <= l1, l2 <= n with two free jobs or more, or a
+			// child range of another size: the father is skipped
+			if (l1 < -1 || l2 > n || u < 2 || A.child_off[f + 1] - c0 != (u == 2 ? 2 : 2 * u)) {
+				__syncthreads();
+				continue;
 			}
-			__syncthreads();
-			continue;
-		}
-		const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
-		// walks: scan all n positions when most jobs are free (more than
-		// 3/4, or half for n > 64 where the position masks take two
-		// words), else follow the position table over the free ones only
-		const bool scan = kWide ? 2 * u > n : 4 * u > 3 * n;
-		if (scan) {
-			if (tid < 4)
-				S.mask[tid] = 0;
-			__syncthreads();
-			if (tid < u)
-				atomicOr(&S.mask[fj[tid] >> 5], 1u << (fj[tid] & 31));
-			__syncthreads();
-		}
-		const uint32_t w0 = S.mask[0], w1 = S.mask[1], w2 = S.mask[2], w3 = S.mask[3];
-		// first chunk: the K ranked pairs (learned) or pairs [0, pc); its
-		// walks overlap the fronts and backs
-		const int len0 = kLearned ? K : min(L.pc, P);
-		if (tid < kFrontThreads) {
-			fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, false);
-		} else {
-			for (int t = tid - kFrontThreads; t < len0; t += kFamThreads - kFrontThreads) {
-				int p = t;
-				if (kLearned)
-					p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
-				if (scan)
-					scan_pair<kWide>(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
-				else
-					walk_pair<kWide>(S, tjT, jobposT, p, t, n, P, xs, fj, u);
-			}
-		}
-		// per job: one thread per (job, slice of the chunk's pairs) takes
-		// both children that move the job
-		const int u32 = (u + 31) & ~31, NS = kFamThreads / u32;
-		const int my_i = tid % u32, my_s = tid / u32;
-		const bool active = my_s < NS && my_i < u;
-		const int my_j = active ? S.fr[l1 + 1 + my_i] : 0;
-		int32_t accB = kNeg, accE = kNeg;
-		__syncthreads();
-		if (active)
-			job_pairs(S, my_s * len0 / NS, (my_s + 1) * len0 / NS, my_j, xs, accB, accE);
-		if (!kLearned) {
-			for (int p_lo = len0; p_lo < P; p_lo += L.pc) {
-				const int len = min(L.pc, P - p_lo);
-				__syncthreads(); // previous chunk consumed
-				for (int t = tid; t < len; t += kFamThreads)
-					{
-					if (scan)
-						scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
-					else
-						walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+			if (u == 2) {
+				// two leaves: makespans of front + (x, y) + back, both orders
+				fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, true);
+				__syncthreads();
+				if (tid < 2) {
+					const int x = S.fr[l1 + 1 + tid], y = S.fr[l1 + 2 - tid];
+					int32_t v1 = 0, v2 = 0, mk = 0;
+					for (int k = 0; k < m; ++k) {
+						v1 = max(v1, S.F[k]) + S.pt[k * (n + 1) + x];
+						v2 = max(v2, v1) + S.pt[k * (n + 1) + y];
+						mk = max(mk, v2 + S.G[m - 1 - k]);
+					}
+					A.child_lb[c0 + tid] = mk;
+					A.child_job[c0 + tid] = int16_t(x);
 				}
 				__syncthreads();
-				if (active)
-					job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, xs, accB, accE);
+				continue;
 			}
-		}
-		__syncthreads(); // the reduction overwrites the X rows
-		S.red[2 * tid] = accB;
-		S.red[2 * tid + 1] = accE;
-		__syncthreads();
-		if (tid < u) {
-			int32_t lbB = S.red[2 * tid], lbE = S.red[2 * tid + 1];
-			for (int s = 1; s < NS; ++s) {
-				lbB = max(lbB, S.red[2 * (s * u32 + tid)]);
-				lbE = max(lbE, S.red[2 * (s * u32 + tid) + 1]);
+			const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
+			// walks: scan all n positions when most jobs are free (more than
+			// 3/4, or half for n > 64 where the position masks take two
+			// words), else follow the position table over the free ones only
+			const bool scan = kWide ? 2 * u > n : 4 * u > 3 * n;
+			if (scan) {
+				if (tid < 4)
+					S.mask[tid] = 0;
+				__syncthreads();
+				if (tid < u)
+					atomicOr(&S.mask[fj[tid] >> 5], 1u << (fj[tid] & 31));
+				__syncthreads();
 			}
-			const int16_t job = S.fr[l1 + 1 + tid];
-			A.child_job[c0 + tid] = job;
-			A.child_job[c0 + u + tid] = job;
-			if (!kLearned) {
-				A.child_lb[c0 + tid] = lbB;
-				A.child_lb[c0 + u + tid] = lbE;
+			const uint32_t w0 = S.mask[0], w1 = S.mask[1], w2 = S.mask[2], w3 = S.mask[3];
+			// first chunk: the K ranked pairs (learned) or pairs [0, pc); its
+			// walks overlap the fronts and backs
+			const int len0 = kLearned ? K : min(L.pc, P);
+			if (tid < kFrontThreads) {
+				fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, false);
 			} else {
-				// settled children keep the bound over the K pairs
-				if (lbB >= thr)
-					A.child_lb[c0 + tid] = lbB;
-				else
-					S.list[atomicAdd(S.cnt, 1)] = int16_t(tid);
-				if (lbE >= thr)
-					A.child_lb[c0 + u + tid] = lbE;
-				else
-					S.list[atomicAdd(S.cnt, 1)] = int16_t(u + tid);
+				for (int t = tid - kFrontThreads; t < len0; t += kFamThreads - kFrontThreads) {
+					int p = t;
+					if (kLearned)
+						p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
+					if (scan)
+						scan_pair<kWide>(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
+					else
+						walk_pair<kWide>(S, tjT, jobposT, p, t, n, P, xs, fj, u);
+				}
 			}
-		}
-		if (kLearned) {
+			// per job: one thread per (job, slice of the chunk's pairs) takes
+			// both children that move the job
+			const int u32 = (u + 31) & ~31, NS = kFamThreads / u32;
+			const int my_i = tid % u32, my_s = tid / u32;
+			const bool active = my_s < NS && my_i < u;
+			const int my_j = active ? S.fr[l1 + 1 + my_i] : 0;
+			int32_t accB = kNeg, accE = kNeg;
 			__syncthreads();
-			const int nu = *S.cnt;
-			if (tid == 0 && 2 * u - nu > 0)
-				atomicAdd(A.early, (unsigned long long)(2 * u - nu));
-			if (tid == 0 && nu == 0 && A.settled_fathers)
-				atomicAdd(A.settled_fathers, 1ull);
-			if (nu > 0) {
-				// the children left: every pair
-				const int nu32 = (nu + 31) & ~31, NS2 = kFamThreads / nu32;
-				const int ci = tid % nu32, cs = tid / nu32;
-				const bool act2 = cs < NS2 && ci < nu;
-				const int c = act2 ? S.list[ci] : 0;
-				const bool begin = c < u;
-				const int j = S.fr[l1 + 1 + (begin ? c : c - u)];
-				int32_t acc = kNeg;
-				for (int p_lo = 0; p_lo < P; p_lo += L.pc) {
+			if (active)
+				job_pairs(S, my_s * len0 / NS, (my_s + 1) * len0 / NS, my_j, xs, accB, accE);
+			if (!kLearned) {
+				for (int p_lo = len0; p_lo < P; p_lo += L.pc) {
 					const int len = min(L.pc, P - p_lo);
-					__syncthreads();
+					__syncthreads(); // previous chunk consumed
 					for (int t = tid; t < len; t += kFamThreads)
 						{
-					if (scan)
-						scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
-					else
-						walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
-				}
+						if (scan)
+							scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+						else
+							walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+					}
 					__syncthreads();
-					if (act2)
-						acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, xs,
-						                  acc);
-				}
-				__syncthreads();
-				S.red[tid] = acc;
-				__syncthreads();
-				if (tid < nu) {
-					int32_t lb = S.red[tid];
-					for (int s = 1; s < NS2; ++s)
-						lb = max(lb, S.red[s * nu32 + tid]);
-					A.child_lb[c0 + S.list[tid]] = lb;
+					if (active)
+						job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, xs, accB, accE);
 				}
 			}
-		}
+			__syncthreads(); // the reduction overwrites the X rows
+			S.red[2 * tid] = accB;
+			S.red[2 * tid + 1] = accE;
+			__syncthreads();
+			if (tid < u) {
+				int32_t lbB = S.red[2 * tid], lbE = S.red[2 * tid + 1];
+				for (int s = 1; s < NS; ++s) {
+					lbB = max(lbB, S.red[2 * (s * u32 + tid)]);
+					lbE = max(lbE, S.red[2 * (s * u32 + tid) + 1]);
+				}
+				const int16_t job = S.fr[l1 + 1 + tid];
+				A.child_job[c0 + tid] = job;
+				A.child_job[c0 + u + tid] = job;
+				if (!kLearned) {
+					A.child_lb[c0 + tid] = lbB;
+					A.child_lb[c0 + u + tid] = lbE;
+				} else {
+					// settled children keep the bound over the K pairs
+					if (lbB >= thr)
+						A.child_lb[c0 + tid] = lbB;
+					else
+						S.list[atomicAdd(S.cnt, 1)] = int16_t(tid);
+					if (lbE >= thr)
+						A.child_lb[c0 + u + tid] = lbE;
+					else
+						S.list[atomicAdd(S.cnt, 1)] = int16_t(u + tid);
+				}
+			}
+			if (kLearned) {
+				__syncthreads();
+				const int nu = *S.cnt;
+				if (tid == 0 && 2 * u - nu > 0)
+					atomicAdd(A.early, (unsigned long long)(2 * u - nu));
+				if (tid == 0 && nu == 0 && A.settled_fathers)
+					atomicAdd(A.settled_fathers, 1ull);
+				if (nu > 0) {
+					// the children left: every pair
+					const int nu32 = (nu + 31) & ~31, NS2 = kFamThreads / nu32;
+					const int ci = tid % nu32, cs = tid / nu32;
+					const bool act2 = cs < NS2 && ci < nu;
+					const int c = act2 ? S.list[ci] : 0;
+					const bool begin = c < u;
+					const int j = S.fr[l1 + 1 + (begin ? c : c - u)];
+					int32_t acc = kNeg;
+					for (int p_lo = 0; p_lo < P; p_lo += L.pc) {
+						const int len = min(L.pc, P - p_lo);
+						__syncthreads();
+						for (int t = tid; t < len; t += kFamThreads)
+							{
+						if (scan)
+							scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
+						else
+							walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+					}
+						__syncthreads();
+						if (act2)
+							acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, xs,
+							                  acc);
+					}
+					__syncthreads();
+					S.red[tid] = acc;
+					__syncthreads();
+					if (tid < nu) {
+						int32_t lb = S.red[tid];
+						for (int s = 1; s < NS2; ++s)
+							lb = max(lb, S.red[s * nu32 + tid]);
+						A.child_lb[c0 + S.list[tid]] = lb;
+					}
+				}
+			}
+			__syncthreads();
+		} while (0);
+		// claim the next father (every thread reads the same value)
+		if (tid == 0)
+			s_next = A.next ? (long long)gridDim.x + (long long)atomicAdd(A.next, 1ull)
+			                : f + gridDim.x;
+		__syncthreads();
+		f = s_next;
 		__syncthreads();
 	}
 }
@@ -682,6 +696,10 @@ extern "C" int wsbb_decompose_lb2(wsbb_ctx *ctx, const void *fathers, int64_t co
 	A.child_lb = child_lb;
 	A.child_job = child_job;
 	A.stride = ctx->bp.stride;
+	A.next = ctx->d_claim;
+	if (e == cudaSuccess && ctx->d_claim)
+		e = cudaMemsetAsync(ctx->d_claim, 0, sizeof(unsigned long long),
+		                    static_cast<cudaStream_t>(stream));
 	if (e == cudaSuccess)
 		e = wsbb::launch_family_lb2(ctx->bp, ctx->tables, A, count, ctx->num_sms,
 		                            static_cast<cudaStream_t>(stream));

@@ -104,6 +104,9 @@ struct FamilyArgs {
 	const int *ub_dev = nullptr, *best_dev = nullptr;
 	unsigned long long *early = nullptr;
 	unsigned long long *settled_fathers = nullptr; // fathers with every child settled
+	// fathers are claimed from this device counter (zero at launch); null:
+	// round-robin by CTA
+	unsigned long long *next = nullptr;
 };
 // smem_kb: shared-memory budget per CTA in KB (0: 56), which sets the
 // pair-chunk length and how many CTAs share an SM.
@@ -162,6 +165,7 @@ struct wsbb_ctx {
 	void *d_recs = nullptr;
 	int32_t *d_out = nullptr;
 	int64_t host_cap = 0;
+	unsigned long long *d_claim = nullptr; // family bounds' father counter
 	cudaStream_t stream = nullptr;
 	// search state (explore.cu)
 	struct ExploreState *ex = nullptr;
