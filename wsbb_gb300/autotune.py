@@ -24,7 +24,7 @@ import os
 import sys
 
 WINDOWS = (512, 1024, 2048, 4096, 8192, 16384, 32768)
-SMEM_KB = (56, 100)
+SMEM_KB = (56, 100, 160)
 
 
 def cache_path() -> str:

@@ -77,7 +77,10 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 	long long pc = budget > off + fixed_after ? (long long)((budget - off - fixed_after) / per_pair)
 	                                          : 0;
 	pc = std::max<long long>(pc, 32);
-	L.pc = int(std::min<long long>(pc, P));
+	// as few chunks as the budget allows, of equal length (a short last
+	// chunk costs a full round of walks and barriers for a few pairs)
+	const long long chunks = (P + pc - 1) / pc;
+	L.pc = int((P + chunks - 1) / chunks);
 	// the per-thread reduction reuses the X rows once the pairs are consumed
 	L.off_X = off;
 	L.off_red = off;
