@@ -71,6 +71,38 @@ def test_family_bounds_match_oracle(env, oracle, n, m, count):
     np.testing.assert_array_equal(job.cpu().numpy(), np.array(moved, dtype=np.int16))
 
 
+@pytest.mark.parametrize("kind", ["int32", "uint16_limit", "uint16_full"])
+def test_family_bounds_time_ranges(env, oracle, kind):
+    """Both slot forms of the family kernel: processing times too large for
+    16-bit bounds ((n + m - 1) * max p > 65535: int32 slots), and instances
+    at the 16-bit limit, where the longest staircase path is 65525."""
+    torch, W = env
+    n, m, count = 20, 6, 120
+    rng = np.random.default_rng({"int32": 1, "uint16_limit": 2, "uint16_full": 3}[kind])
+    if kind == "int32":
+        p = rng.integers(1, 5001, (m, n)).astype(np.int32)
+    elif kind == "uint16_limit":
+        p = rng.integers(1, 2622, (m, n)).astype(np.int32)
+        p[:, ::3] = 2621
+    else:
+        p = np.full((m, n), 2621, dtype=np.int32)    # every makespan is 25 * 2621
+    ctx = W.Context(p)
+    perms, l1, l2 = random_fathers(rng, n, count)
+    fathers = W.pack_records(perms, l1, l2)
+    kids, off = W.expand_children(fathers, n)
+    d_f = torch.from_numpy(fathers).cuda()
+    d_off = torch.from_numpy(off).cuda()
+    lb = torch.full((len(kids),), -7, dtype=torch.int32, device="cuda")
+    job = torch.full((len(kids),), -7, dtype=torch.int16, device="cuda")
+    ctx.decompose_lb2(d_f.data_ptr(), count, d_off.data_ptr(), lb.data_ptr(), job.data_ptr())
+    torch.cuda.synchronize()
+    kp, k1, k2 = W.unpack_records(kids, n)
+    want = oracle.Bound(p).eval_batch(kp, k1, k2)
+    if kind == "uint16_full":
+        assert want.max() == 25 * 2621
+    np.testing.assert_array_equal(lb.cpu().numpy(), want)
+
+
 def test_family_bounds_equal_per_child_kernel(env):
     """Same bounds as the pool kernel on the expanded children, at a pool
     size where every CTA takes many fathers."""

@@ -1,5 +1,6 @@
 // C-ABI entry points (include/wsbb_gb300.h): context set-up (instance
 // precompute + device tables), pool bounds on device or host buffers.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -114,6 +115,10 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 	for (int32_t v : ctx->inst.p)
 		total += v;
 	bp.col16 = total < 32768 ? 1 : 0;
+	int32_t pmax = 0;
+	for (int32_t v : ctx->inst.p)
+		pmax = std::max(pmax, v);
+	bp.span16 = int64_t(n + m - 1) * pmax <= 65535 ? 1 : 0;
 	*out = ctx;
 	return WSBB_OK;
 }

@@ -37,6 +37,20 @@
 // Child order (the search's, make_children_kernel): the u BEGIN children
 // (free position l1+1+k moved to the front) then the u END children
 // (position l1+1+k moved to the back); two leaves for a simple father.
+//
+// Work split in a CTA (one father at a time): warps 0-1 compute the fronts
+// and backs while warps 2-7 run the forward pass of each pair (thread per
+// pair); after a barrier the same threads run the backward pass, and at
+// job j, the moment X_j is known, bound both children that move j for the
+// pair and store the two values in the pair's row (column j). A last
+// sweep takes, per child, the maximum over the rows. With no back jobs the
+// reference's pair value is t1 + tails[m2]; here the back term of m1 is 0,
+// which gives the same maximum because t0 <= t1 once one job has been
+// walked (t1 >= t0 + lag + b after every step) and tails >= 0. Every value
+// is then a staircase-path length of some permutation, at most
+// (n + m - 1) * max p, so when that fits 16 bits both children's values
+// share one 32-bit slot (BoundParams::span16) and the sweep is one
+// two-halves max per slot.
 #include <algorithm>
 
 #include "wsbb_internal.h"
@@ -46,19 +60,56 @@ namespace {
 
 constexpr int kFamThreads = 256;
 constexpr int kFrontThreads = 64; // warps 0-1: fronts and backs, while the rest walk pairs
+constexpr int kWalkThreads = kFamThreads - kFrontThreads;
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
-struct FamLayout {
-	int xs; // X row stride (odd: rows of consecutive pairs start in different banks)
-	int pc; // pairs per chunk
-	size_t off_pairs, off_V, off_W, off_PF, off_PR, off_X, off_PI, off_red, off_F, off_G, off_fr,
-	    off_list, off_misc, bytes;
+// One X slot: the forward pass leaves C of the prefix before the job there;
+// the backward pass replaces it with the bounds of the job's BEGIN and END
+// children for the pair.
+template <bool k16>
+struct Slot;
+template <>
+struct Slot<true> { // both bounds as uint16 halves (BEGIN low, END high)
+	using T = uint32_t;
+	static __device__ __forceinline__ T pre(int32_t c) { return uint32_t(c); }
+	static __device__ __forceinline__ int32_t pre_of(T s) { return int32_t(s); }
+	static __device__ __forceinline__ T pack(int32_t b, int32_t e)
+	{
+		return __byte_perm(uint32_t(b), uint32_t(e), 0x5410);
+	}
+	static __device__ __forceinline__ T none() { return 0u; } // every bound is >= 0
+	static __device__ __forceinline__ T vmax(T a, T b) { return __vmaxu2(a, b); }
+	static __device__ __forceinline__ int32_t begin(T s) { return int32_t(s & 0xffffu); }
+	static __device__ __forceinline__ int32_t end(T s) { return int32_t(s >> 16); }
+};
+template <>
+struct Slot<false> {
+	using T = int2;
+	static __device__ __forceinline__ T pre(int32_t c) { return make_int2(c, 0); }
+	static __device__ __forceinline__ int32_t pre_of(T s) { return s.x; }
+	static __device__ __forceinline__ T pack(int32_t b, int32_t e) { return make_int2(b, e); }
+	static __device__ __forceinline__ T none() { return make_int2(kNeg, kNeg); }
+	static __device__ __forceinline__ T vmax(T a, T b)
+	{
+		return make_int2(max(a.x, b.x), max(a.y, b.y));
+	}
+	static __device__ __forceinline__ int32_t begin(T s) { return s.x; }
+	static __device__ __forceinline__ int32_t end(T s) { return s.y; }
 };
 
-FamLayout fam_layout(int n, int m, int P, size_t budget)
+struct FamLayout {
+	int xs;   // X row stride in slots (odd: rows of consecutive pairs start in different banks)
+	int pc;   // pairs per chunk
+	int slot; // bytes per X slot (4: packed 16-bit bounds, 8: int32 bounds)
+	size_t off_pairs, off_V, off_W, off_PFR, off_X, off_PI, off_red, off_F, off_G, off_fr,
+	    off_misc, bytes;
+};
+
+FamLayout fam_layout(int n, int m, int P, size_t budget, bool pack16)
 {
 	FamLayout L;
 	L.xs = n | 1;
+	L.slot = pack16 ? 4 : 8;
 	auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
 	// pt as uint16 (the tables cap times at 65535), rows of n + 1 like V and W
 	size_t off = a16(size_t(m) * (n + 1) * 2);
@@ -68,12 +119,10 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 	off = a16(off + size_t(m) * (n + 1) * 4);
 	L.off_W = off;
 	off = a16(off + size_t(m) * (n + 1) * 4);
-	L.off_PF = off;
-	off = a16(off + size_t(P) * 8);
-	L.off_PR = off;
-	off = a16(off + size_t(P) * 8);
-	const size_t fixed_after = a16(32 * 4) * 2 + a16(size_t(n + 4) * 2) + a16(size_t(2 * n) * 2) + 32;
-	const size_t per_pair = size_t(L.xs) * 4 + 16;
+	L.off_PFR = off;
+	off = a16(off + size_t(P) * 16);
+	const size_t fixed_after = a16(32 * 4) * 2 + a16(size_t(n + 4) * 2) + 32;
+	const size_t per_pair = size_t(L.xs) * L.slot + 16;
 	long long pc = budget > off + fixed_after ? (long long)((budget - off - fixed_after) / per_pair)
 	                                          : 0;
 	pc = std::max<long long>(pc, 32);
@@ -81,10 +130,10 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 	// chunk costs a full round of walks and barriers for a few pairs)
 	const long long chunks = (P + pc - 1) / pc;
 	L.pc = int((P + chunks - 1) / chunks);
-	// the per-thread reduction reuses the X rows once the pairs are consumed
+	// the cross-slice reduction reuses the X rows once the chunk is consumed
 	L.off_X = off;
 	L.off_red = off;
-	off = a16(off + std::max(size_t(L.pc) * L.xs * 4, size_t(2 * kFamThreads * 4)));
+	off = a16(off + std::max(size_t(L.pc) * L.xs, size_t(kFamThreads)) * L.slot);
 	L.off_PI = off;
 	off = a16(off + size_t(L.pc) * 16);
 	L.off_F = off;
@@ -93,8 +142,6 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 	off = a16(off + 32 * 4);
 	L.off_fr = off;
 	off = a16(off + size_t(n + 4) * 2);
-	L.off_list = off;
-	off = a16(off + size_t(2 * n) * 2);
 	L.off_misc = off;
 	off += 32;
 	L.bytes = a16(off);
@@ -103,10 +150,11 @@ FamLayout fam_layout(int n, int m, int P, size_t budget)
 
 struct FamSmem {
 	uint16_t *pt;
-	int32_t *pairs, *V, *W, *X, *red, *F, *G;
-	int2 *PF, *PR;
-	int4 *PI;
-	int16_t *fr, *list;
+	int32_t *pairs, *V, *W, *F, *G;
+	int4 *PFR; // per pair: the father's front (m1, m2) and back (m1, m2) times
+	int4 *PI;  // per chunk slot: (m1 (n+1) | m2 (n+1) << 16, A, B, pair)
+	uint8_t *X, *red;
+	int16_t *fr;
 	uint32_t *mask; // [4] free jobs (scan walks)
 	int *cnt;       // [1]
 };
@@ -118,15 +166,13 @@ __device__ __forceinline__ FamSmem carve(uint8_t *smem, const FamLayout &L)
 	S.pairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
 	S.V = reinterpret_cast<int32_t *>(smem + L.off_V);
 	S.W = reinterpret_cast<int32_t *>(smem + L.off_W);
-	S.PF = reinterpret_cast<int2 *>(smem + L.off_PF);
-	S.PR = reinterpret_cast<int2 *>(smem + L.off_PR);
-	S.X = reinterpret_cast<int32_t *>(smem + L.off_X);
+	S.PFR = reinterpret_cast<int4 *>(smem + L.off_PFR);
+	S.X = smem + L.off_X;
 	S.PI = reinterpret_cast<int4 *>(smem + L.off_PI);
-	S.red = reinterpret_cast<int32_t *>(smem + L.off_red);
+	S.red = smem + L.off_red;
 	S.F = reinterpret_cast<int32_t *>(smem + L.off_F);
 	S.G = reinterpret_cast<int32_t *>(smem + L.off_G);
 	S.fr = reinterpret_cast<int16_t *>(smem + L.off_fr);
-	S.list = reinterpret_cast<int16_t *>(smem + L.off_list);
 	S.mask = reinterpret_cast<uint32_t *>(smem + L.off_misc);
 	S.cnt = reinterpret_cast<int *>(smem + L.off_misc + 16);
 	return S;
@@ -135,15 +181,16 @@ __device__ __forceinline__ FamSmem carve(uint8_t *smem, const FamLayout &L)
 // Warp 0: the father's raw front F (a wavefront, lane = machine: lane k
 // takes job s - k at step s), the children's inherited front (column n of
 // V: F or the static heads), every BEGIN child's front (column j: F
-// followed by job j) and the per-pair (F[m1], F[m2]). Warp 1: the same for
-// the reversed back G, W and (back[m1] or -inf without back jobs, back[m2]).
-// With `leaves_only`, F and G only.
+// followed by job j) and the per-pair front (F[m1], F[m2]). Warp 1: the
+// same for the reversed back G, W and the per-pair back (back[m1], or 0
+// without back jobs, and back[m2]). With `leaves_only`, F and G only.
 __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int lane, int n,
                                                  int m, int P, int l1, int l2, int u,
                                                  const int32_t *heads, const int32_t *tails,
                                                  bool leaves_only)
 {
 	const int ld = n + 1;
+	int2 *pfr = reinterpret_cast<int2 *>(S.PFR);
 	if (warp == 0) {
 		int32_t Fk = 0;
 		const int nj = l1 + 1;
@@ -174,7 +221,7 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 		}
 		for (int p = lane; p < P; p += 32) {
 			const int pr = S.pairs[p];
-			S.PF[p] = make_int2(S.V[(pr & 0xff) * ld + n], S.V[(pr >> 8) * ld + n]);
+			pfr[2 * p] = make_int2(S.V[(pr & 0xff) * ld + n], S.V[(pr >> 8) * ld + n]);
 		}
 	} else if (warp == 1) {
 		int32_t Gq = 0;
@@ -208,12 +255,13 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 		for (int p = lane; p < P; p += 32) {
 			const int pr = S.pairs[p];
 			const int32_t r1 = S.W[(pr & 0xff) * ld + n];
-			S.PR[p] = make_int2(l2 < n ? r1 : kNeg, S.W[(pr >> 8) * ld + n]);
+			pfr[2 * p + 1] = make_int2(l2 < n ? r1 : 0, S.W[(pr >> 8) * ld + n]);
 		}
 	}
 }
 
 constexpr int kWalkBatch = 4;
+constexpr int kScanBatch = 8;
 
 // The next free position of a pair's Johnson order (ascending or
 // descending) from its free-position mask (w0: positions 0-63, w1: 64-127);
@@ -251,83 +299,19 @@ __device__ __forceinline__ int next_down(uint64_t &w0, uint64_t &w1)
 }
 
 template <bool kWide>
-__device__ __forceinline__ bool free_bit(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
-                                         int job)
+__device__ __forceinline__ bool free_bit(const uint32_t *w, int job)
 {
-	const uint32_t lo = (job & 32) ? w1 : w0;
-	if (!kWide) // n <= 64
-		return ((lo >> (job & 31)) & 1u) != 0;
-	const uint32_t hi = (job & 32) ? w3 : w2;
-	return ((((job & 64) ? hi : lo) >> (job & 31)) & 1u) != 0;
+	return ((w[(kWide ? job & 127 : job & 63) >> 5] >> (job & 31)) & 1u) != 0;
 }
 
-constexpr int kScanBatch = 8;
-
-// The same passes as walk_pair below, scanning all n positions of the
-// order and skipping the fixed jobs (free-job mask w0..w3): cheaper than
-// the position-table walk when almost every job is free.
+// Positions of the father's free jobs in pair p's Johnson order, as a mask
+// (u lookups in the job-position table).
 template <bool kWide>
-__device__ __forceinline__ void scan_pair(const FamSmem &S, const uint2 *__restrict__ tjT, int p,
-                                          int slot, int n, int P, int xs, uint32_t w0,
-                                          uint32_t w1, uint32_t w2, uint32_t w3)
+__device__ __forceinline__ void walk_mask(const uint8_t *__restrict__ jobposT, const int16_t *fj,
+                                          int u, int p, int P, uint64_t &m0, uint64_t &m1)
 {
-	const uint2 *e = tjT + p;
-	int32_t *xrow = S.X + slot * xs;
-	int32_t a_sum = 0, b_sum = 0, c = kNeg;
-	for (int q0 = 0; q0 < n; q0 += kScanBatch) {
-		uint2 v[kScanBatch];
-#pragma unroll
-		for (int k = 0; k < kScanBatch; ++k)
-			v[k] = q0 + k < n ? __ldg(e + (size_t)(q0 + k) * P) : make_uint2(0u, 0u);
-#pragma unroll
-		for (int k = 0; k < kScanBatch; ++k) {
-			const int job = int(v[k].x & 0xffu);
-			if (q0 + k < n && free_bit<kWide>(w0, w1, w2, w3, job)) {
-				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
-				const int32_t cj = int32_t(v[k].y >> 16);
-				xrow[job] = c;
-				c = max(c + b, a_sum + cj);
-				a_sum += a;
-				b_sum += b;
-			}
-		}
-	}
-	const int pr = S.pairs[p], ld = n + 1;
-	S.PI[slot] = make_int4((pr & 0xff) * ld | ((pr >> 8) * ld) << 16, a_sum, b_sum, p);
-	int32_t as = 0, bs = 0, cs = kNeg;
-	for (int q0 = n - 1; q0 >= 0; q0 -= kScanBatch) {
-		uint2 v[kScanBatch];
-#pragma unroll
-		for (int k = 0; k < kScanBatch; ++k)
-			v[k] = q0 - k >= 0 ? __ldg(e + (size_t)(q0 - k) * P) : make_uint2(0u, 0u);
-#pragma unroll
-		for (int k = 0; k < kScanBatch; ++k) {
-			const int job = int(v[k].x & 0xffu);
-			if (q0 - k >= 0 && free_bit<kWide>(w0, w1, w2, w3, job)) {
-				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
-				const int32_t cj = int32_t(v[k].y >> 16);
-				const int32_t apre = a_sum - as - a;
-				xrow[job] = max(xrow[job] + bs, apre + cs);
-				cs = max(cs + a, bs + cj);
-				as += a;
-				bs += b;
-			}
-		}
-	}
-}
-
-// Pair p's forward and backward max-plus passes over its Johnson order,
-// restricted to the father's u free jobs `fj`: X[slot][j] = C of (suffix
-// after j) x (prefix before j), and PI[slot] = (m1 (n+1) | m2 (n+1) << 16,
-// A, B, p): the row offsets of the pair's machines in pt, V and W. The
-// free positions come from the job-position table (u lookups, not a scan
-// of all n positions), so both passes touch only the u free entries.
-template <bool kWide>
-__device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restrict__ tjT,
-                                          const uint8_t *__restrict__ jobposT, int p, int slot,
-                                          int n, int P, int xs, const int16_t *fj, int u)
-{
-	uint64_t m0 = 0, m1 = 0;
+	m0 = 0;
+	m1 = 0;
 #pragma unroll 8
 	for (int i = 0; i < u; ++i) {
 		const int q = __ldg(jobposT + (size_t)fj[i] * P + p);
@@ -339,114 +323,182 @@ __device__ __forceinline__ void walk_pair(const FamSmem &S, const uint2 *__restr
 			m0 |= 1ull << q;
 		}
 	}
-	const uint2 *e = tjT + p;
-	int32_t *xrow = S.X + slot * xs;
+}
+
+// body(entry) for each of the father's free jobs in a pair's Johnson order
+// (entries e[q * P], q = position), ascending (kUp) or descending. Walk
+// form: the set bits of the position mask (m0, m1), u of them. Scan form:
+// all n positions, keeping the entries whose job is in the free-job mask w
+// (cheaper when almost every job is free).
+template <bool kUp, bool kScan, bool kWide, typename Body>
+__device__ __forceinline__ void each_free(const uint2 *__restrict__ e, int n, int P, int u,
+                                          uint64_t m0, uint64_t m1, const uint32_t *w,
+                                          Body &&body)
+{
+	if (kScan) {
+		for (int k0 = 0; k0 < n; k0 += kScanBatch) {
+			uint2 v[kScanBatch];
+#pragma unroll
+			for (int k = 0; k < kScanBatch; ++k) {
+				const int q = kUp ? k0 + k : n - 1 - k0 - k;
+				v[k] = k0 + k < n ? __ldg(e + (size_t)q * P) : make_uint2(0u, 0u);
+			}
+#pragma unroll
+			for (int k = 0; k < kScanBatch; ++k)
+				if (k0 + k < n && free_bit<kWide>(w, int(v[k].x & 0xffu)))
+					body(v[k]);
+		}
+	} else {
+		for (int left = u; left > 0; left -= kWalkBatch) {
+			int q[kWalkBatch];
+			uint2 v[kWalkBatch];
+#pragma unroll
+			for (int k = 0; k < kWalkBatch; ++k)
+				q[k] = kUp ? next_up<kWide>(m0, m1) : next_down<kWide>(m0, m1);
+#pragma unroll
+			for (int k = 0; k < kWalkBatch; ++k)
+				v[k] = q[k] >= 0 ? __ldg(e + (size_t)q[k] * P) : make_uint2(0u, 0u);
+#pragma unroll
+			for (int k = 0; k < kWalkBatch; ++k)
+				if (q[k] >= 0)
+					body(v[k]);
+		}
+	}
+}
+
+// Entry fields: x = job | a << 16, y = b | c << 16 (a = p[m1][job],
+// b = p[m2][job], c = a + lag + b).
+#define WSBB_ENTRY(v)                                                         \
+	const int job = int((v).x & 0xffu);                                       \
+	const int32_t a = int32_t((v).x >> 16), b = int32_t((v).y & 0xffffu);    \
+	const int32_t cj = int32_t((v).y >> 16)
+
+// Forward pass of pair p (chunk slot t): X[t][j] = C of the free jobs
+// before j; PI[t] = (row offsets of m1, m2, A, B, p).
+template <bool kScan, bool kWide, bool k16>
+__device__ __forceinline__ void pair_forward(const FamSmem &S, const uint2 *__restrict__ tjT,
+                                             int p, int t, int n, int P, int xs, int u,
+                                             uint64_t m0, uint64_t m1, const uint32_t *w)
+{
+	using Sl = Slot<k16>;
+	typename Sl::T *xrow = reinterpret_cast<typename Sl::T *>(S.X) + t * xs;
 	int32_t a_sum = 0, b_sum = 0, c = kNeg;
-	uint64_t w0 = m0, w1 = m1;
-	for (int left = u; left > 0; left -= kWalkBatch) {
-		int q[kWalkBatch];
-		uint2 v[kWalkBatch];
-#pragma unroll
-		for (int k = 0; k < kWalkBatch; ++k)
-			q[k] = next_up<kWide>(w0, w1);
-#pragma unroll
-		for (int k = 0; k < kWalkBatch; ++k)
-			v[k] = q[k] >= 0 ? __ldg(e + (size_t)q[k] * P) : make_uint2(0u, 0u);
-#pragma unroll
-		for (int k = 0; k < kWalkBatch; ++k) {
-			if (q[k] >= 0) {
-				const int job = int(v[k].x & 0xffu);
-				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
-				const int32_t cj = int32_t(v[k].y >> 16); // a + lag + b
-				xrow[job] = c; // C of the prefix before job
-				c = max(c + b, a_sum + cj);
-				a_sum += a;
-				b_sum += b;
-			}
-		}
-	}
+	each_free<true, kScan, kWide>(tjT + p, n, P, u, m0, m1, w, [&](uint2 v) {
+		WSBB_ENTRY(v);
+		xrow[job] = Sl::pre(c);
+		c = max(c + b, a_sum + cj);
+		a_sum += a;
+		b_sum += b;
+	});
 	const int pr = S.pairs[p], ld = n + 1;
-	S.PI[slot] = make_int4((pr & 0xff) * ld | ((pr >> 8) * ld) << 16, a_sum, b_sum, p);
+	S.PI[t] = make_int4((pr & 0xff) * ld | ((pr >> 8) * ld) << 16, a_sum, b_sum, p);
+}
+
+// Backward pass of chunk slot t: at each free job j, X_j = C of (the free
+// jobs after j) x (those before j), then both children that move j:
+//   BEGIN (front V[.][j], the father's back r):
+//     max(v2 + B - b + r2, v1 + X_j + r2, v1 + A - a + r1)
+//   END (the father's front f, back W[.][j]):
+//     max(w2 + B - b + f2, w2 + X_j + f1, w1 + A - a + f1)
+// (t0 = v1 + A - a, t1 = max(v2 + B - b, v1 + X_j), bound max(t1 + r2,
+// t0 + r1), expanded), stored in X[t][j].
+template <bool kScan, bool kWide, bool k16>
+__device__ __forceinline__ void pair_backward(const FamSmem &S, const uint2 *__restrict__ tjT,
+                                              int t, int n, int P, int xs, int u, uint64_t m0,
+                                              uint64_t m1, const uint32_t *w)
+{
+	using Sl = Slot<k16>;
+	typename Sl::T *xrow = reinterpret_cast<typename Sl::T *>(S.X) + t * xs;
+	const int4 pi = S.PI[t];
+	const int4 fr = S.PFR[pi.w]; // (f1, f2, r1, r2)
+	const int row1 = pi.x & 0xffff, row2 = int(unsigned(pi.x) >> 16);
+	const int32_t A = pi.y, B = pi.z;
+	const int32_t kb1 = B + fr.w, kb2 = A + fr.z, ke1 = B + fr.y, ke2 = A + fr.x;
 	int32_t as = 0, bs = 0, cs = kNeg;
-	w0 = m0;
-	w1 = m1;
-	for (int left = u; left > 0; left -= kWalkBatch) {
-		int q[kWalkBatch];
-		uint2 v[kWalkBatch];
-#pragma unroll
-		for (int k = 0; k < kWalkBatch; ++k)
-			q[k] = next_down<kWide>(w0, w1);
-#pragma unroll
-		for (int k = 0; k < kWalkBatch; ++k)
-			v[k] = q[k] >= 0 ? __ldg(e + (size_t)q[k] * P) : make_uint2(0u, 0u);
-#pragma unroll
-		for (int k = 0; k < kWalkBatch; ++k) {
-			if (q[k] >= 0) {
-				const int job = int(v[k].x & 0xffu);
-				const int32_t a = int32_t(v[k].x >> 16), b = int32_t(v[k].y & 0xffffu);
-				const int32_t cj = int32_t(v[k].y >> 16);
-				const int32_t apre = a_sum - as - a;
-				xrow[job] = max(xrow[job] + bs, apre + cs);
-				cs = max(cs + a, bs + cj);
-				as += a;
-				bs += b;
+	each_free<false, kScan, kWide>(tjT + pi.w, n, P, u, m0, m1, w, [&](uint2 v) {
+		WSBB_ENTRY(v);
+		const int32_t x = max(Sl::pre_of(xrow[job]) + bs, (A - as - a) + cs);
+		cs = max(cs + a, bs + cj);
+		as += a;
+		bs += b;
+		const int32_t v1 = S.V[row1 + job], v2 = S.V[row2 + job];
+		const int32_t w1 = S.W[row1 + job], w2 = S.W[row2 + job];
+		const int32_t tb = max(max(v2 - b + kb1, v1 + x + fr.w), v1 - a + kb2);
+		const int32_t te = max(max(w2 - b + ke1, w2 + x + fr.x), w1 - a + ke2);
+		xrow[job] = Sl::pack(tb, te);
+	});
+}
+#undef WSBB_ENTRY
+
+// Bounds of the father's children over one chunk of pairs (slot t holds
+// pair fp[t] when fp is set, else p_lo + t), folded into `acc` for the
+// calling thread's job column rj and its slice of slots. The front
+// threads compute the fronts and backs first when `fronts` is set. Called
+// by every thread; X must be free on entry.
+template <bool kWide, bool k16>
+__device__ __forceinline__ void chunk_bounds(const FamSmem &S, const uint2 *__restrict__ tjT,
+                                             const uint8_t *__restrict__ jobposT,
+                                             const BoundParams &bp, const int16_t *fp, int p_lo,
+                                             int len, bool fronts, bool scan, int xs, int l1,
+                                             int l2, int u, bool ract, int rj, int rlo, int rhi,
+                                             typename Slot<k16>::T &acc)
+{
+	using Sl = Slot<k16>;
+	const int tid = threadIdx.x, n = bp.n, m = bp.m, P = bp.P;
+	const uint32_t *w = S.mask;
+	const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
+	uint64_t km0 = 0, km1 = 0;          // the walk mask of a walker's single pair
+	if (tid < kFrontThreads) {
+		if (fronts)
+			fronts_and_backs(S, tid >> 5, tid & 31, n, m, P, l1, l2, u,
+			                 reinterpret_cast<const int32_t *>(bp.t8.blob + bp.t8.off_heads),
+			                 reinterpret_cast<const int32_t *>(bp.t8.blob + bp.t8.off_tails),
+			                 false);
+	} else {
+		for (int t = tid - kFrontThreads; t < len; t += kWalkThreads) {
+			const int p = fp ? min(max(int(fp[t]), 0), P - 1) : p_lo + t;
+			if (scan) {
+				pair_forward<true, kWide, k16>(S, tjT, p, t, n, P, xs, u, 0, 0, w);
+			} else {
+				walk_mask<kWide>(jobposT, fj, u, p, P, km0, km1);
+				pair_forward<false, kWide, k16>(S, tjT, p, t, n, P, xs, u, km0, km1, w);
 			}
 		}
 	}
-}
-
-// Both children that move job j (BEGIN and END) over chunk slots [lo, hi).
-__device__ __forceinline__ void job_pairs(const FamSmem &S, int lo, int hi, int j, int xs,
-                                          int32_t &accB, int32_t &accE)
-{
-	const int32_t *xp = S.X + lo * xs + j;
-	for (int t = lo; t < hi; ++t, xp += xs) {
-		const int4 pi = S.PI[t];
-		const int o1 = (pi.x & 0xffff) + j, o2 = (int(unsigned(pi.x) >> 16)) + j;
-		const int2 pf = S.PF[pi.w], pr = S.PR[pi.w];
-		const int32_t x = *xp;
-		const int32_t aa = pi.y - int32_t(S.pt[o1]), bb = pi.z - int32_t(S.pt[o2]);
-		// BEGIN child: front V[.][j], the father's back
-		const int32_t v1 = S.V[o1], v2 = S.V[o2];
-		const int32_t t0 = v1 + aa, t1 = max(v2 + bb, v1 + x);
-		accB = max(accB, max(t1 + pr.y, t0 + pr.x));
-		// END child: the father's front, back W[.][j]
-		const int32_t w1 = S.W[o1], w2 = S.W[o2];
-		const int32_t e0 = pf.x + aa, e1 = max(pf.y + bb, pf.x + x);
-		accE = max(accE, max(e1 + w2, e0 + w1));
+	__syncthreads(); // fronts, backs and every forward pass done
+	if (tid >= kFrontThreads) {
+		for (int t = tid - kFrontThreads; t < len; t += kWalkThreads) {
+			if (scan) {
+				pair_backward<true, kWide, k16>(S, tjT, t, n, P, xs, u, 0, 0, w);
+			} else {
+				// a walker with several pairs rebuilds each one's mask
+				if (len > kWalkThreads)
+					walk_mask<kWide>(jobposT, fj, u, S.PI[t].w, P, km0, km1);
+				pair_backward<false, kWide, k16>(S, tjT, t, n, P, xs, u, km0, km1, w);
+			}
+		}
 	}
-}
-
-// One child (c < u: BEGIN, else END) over chunk slots [lo, hi).
-__device__ __forceinline__ int32_t child_pairs(const FamSmem &S, int lo, int hi, int j,
-                                               bool begin, int xs, int32_t acc)
-{
-	const int32_t *xp = S.X + lo * xs + j;
-	for (int t = lo; t < hi; ++t, xp += xs) {
-		const int4 pi = S.PI[t];
-		const int o1 = (pi.x & 0xffff) + j, o2 = (int(unsigned(pi.x) >> 16)) + j;
-		const int32_t x = *xp;
-		const int32_t aa = pi.y - int32_t(S.pt[o1]), bb = pi.z - int32_t(S.pt[o2]);
-		const int2 pf = S.PF[pi.w], pr = S.PR[pi.w];
-		// BEGIN: own front, the father's back; END: the father's front, own back
-		const int32_t v1 = begin ? S.V[o1] : pf.x, v2 = begin ? S.V[o2] : pf.y;
-		const int32_t r1 = begin ? pr.x : S.W[o1], r2 = begin ? pr.y : S.W[o2];
-		const int32_t t0 = v1 + aa, t1 = max(v2 + bb, v1 + x);
-		acc = max(acc, max(t1 + r2, t0 + r1));
+	__syncthreads();
+	if (ract) {
+		const typename Sl::T *col = reinterpret_cast<const typename Sl::T *>(S.X) + rj;
+		const int lo = rlo * len / rhi, hi = (rlo + 1) * len / rhi;
+		for (int t = lo; t < hi; ++t)
+			acc = Sl::vmax(acc, col[t * xs]);
 	}
-	return acc;
 }
 
 // kLearned: the father's K ranked pairs first; a child whose bound over
 // them reaches max(best, incumbent) is settled with that value (the search
 // only compares such bounds with the thresholds, never ranks or sums
-// them); fathers with children left walk every pair for those children.
-template <bool kLearned, bool kWide>
+// them); fathers with children left take every pair for those children.
+template <bool kLearned, bool kWide, bool k16>
 __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, BoundParams bp,
                                                              const uint2 *__restrict__ tjT,
                                                              const uint8_t *__restrict__ jobposT,
                                                              FamLayout L)
 {
+	using Sl = Slot<k16>;
+	using T = typename Sl::T;
 	extern __shared__ __align__(16) uint8_t smem[];
 	const long long nf = A.count_dev ? *A.count_dev : A.count;
 	if ((long long)blockIdx.x >= nf)
@@ -466,7 +518,9 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 	const int32_t *heads = reinterpret_cast<const int32_t *>(tb + bp.t8.off_heads);
 	const int32_t *tails = reinterpret_cast<const int32_t *>(tb + bp.t8.off_tails);
 	const int thr = kLearned ? max(*A.best_dev, *A.ub_dev) : 0;
-	const int K = kLearned ? min(A.K, P) : 0;
+	// the K ranked pairs form one chunk
+	const int K = kLearned ? min(min(A.K, P), L.pc) : 0;
+	T *red = reinterpret_cast<T *>(S.red);
 
 	// fathers: the CTA's own first, then the next unclaimed one from the
 	// device counter (A.next, zero at launch), so CTAs that drew light
@@ -511,7 +565,6 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 				__syncthreads();
 				continue;
 			}
-			const int16_t *fj = S.fr + l1 + 1; // the father's free jobs
 			// walks: scan all n positions when most jobs are free (more than
 			// 3/4, or half for n > 64 where the position masks take two
 			// words), else follow the position table over the free ones only
@@ -521,121 +574,80 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 					S.mask[tid] = 0;
 				__syncthreads();
 				if (tid < u)
-					atomicOr(&S.mask[fj[tid] >> 5], 1u << (fj[tid] & 31));
+					atomicOr(&S.mask[S.fr[l1 + 1 + tid] >> 5], 1u << (S.fr[l1 + 1 + tid] & 31));
 				__syncthreads();
 			}
-			const uint32_t w0 = S.mask[0], w1 = S.mask[1], w2 = S.mask[2], w3 = S.mask[3];
-			// first chunk: the K ranked pairs (learned) or pairs [0, pc); its
-			// walks overlap the fronts and backs
-			const int len0 = kLearned ? K : min(L.pc, P);
-			if (tid < kFrontThreads) {
-				fronts_and_backs(S, warp, lane, n, m, P, l1, l2, u, heads, tails, false);
-			} else {
-				for (int t = tid - kFrontThreads; t < len0; t += kFamThreads - kFrontThreads) {
-					int p = t;
-					if (kLearned)
-						p = min(max(int(A.fpairs[f * A.K + t]), 0), P - 1);
-					if (scan)
-						scan_pair<kWide>(S, tjT, p, t, n, P, xs, w0, w1, w2, w3);
-					else
-						walk_pair<kWide>(S, tjT, jobposT, p, t, n, P, xs, fj, u);
+			// the final sweep: thread (free job tid % u, slice rs) of NS slices
+			const int NS = min(kFamThreads / u, 32);
+			const int rs = tid / u;
+			const bool ract = rs < NS;
+			const int rj = ract ? S.fr[l1 + 1 + tid % u] : 0;
+			T acc = Sl::none();
+			int32_t lbB = 0, lbE = 0;
+			bool needB = true, needE = true;
+			if (kLearned) {
+				chunk_bounds<kWide, k16>(S, tjT, jobposT, bp, A.fpairs + f * A.K, 0, K, true, scan,
+				                         xs, l1, l2, u, ract, rj, rs, NS, acc);
+				__syncthreads(); // red overwrites the X rows
+				red[tid] = acc;
+				__syncthreads();
+				int nu = 0;
+				if (tid < u) {
+					T s = red[tid];
+					for (int k = 1; k < NS; ++k)
+						s = Sl::vmax(s, red[k * u + tid]);
+					lbB = Sl::begin(s);
+					lbE = Sl::end(s);
+					// settled children keep the bound over the K pairs
+					needB = lbB < thr;
+					needE = lbE < thr;
+					if (!needB)
+						A.child_lb[c0 + tid] = lbB;
+					if (!needE)
+						A.child_lb[c0 + u + tid] = lbE;
+					nu = int(needB) + int(needE);
+					if (nu)
+						atomicAdd(S.cnt, nu);
 				}
-			}
-			// per job: one thread per (job, slice of the chunk's pairs) takes
-			// both children that move the job
-			const int u32 = (u + 31) & ~31, NS = kFamThreads / u32;
-			const int my_i = tid % u32, my_s = tid / u32;
-			const bool active = my_s < NS && my_i < u;
-			const int my_j = active ? S.fr[l1 + 1 + my_i] : 0;
-			int32_t accB = kNeg, accE = kNeg;
-			__syncthreads();
-			if (active)
-				job_pairs(S, my_s * len0 / NS, (my_s + 1) * len0 / NS, my_j, xs, accB, accE);
-			if (!kLearned) {
-				for (int p_lo = len0; p_lo < P; p_lo += L.pc) {
-					const int len = min(L.pc, P - p_lo);
-					__syncthreads(); // previous chunk consumed
-					for (int t = tid; t < len; t += kFamThreads)
-						{
-						if (scan)
-							scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
-						else
-							walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
+				__syncthreads();
+				const int left = *S.cnt;
+				if (tid == 0 && 2 * u - left > 0)
+					atomicAdd(A.early, (unsigned long long)(2 * u - left));
+				if (tid == 0 && left == 0 && A.settled_fathers)
+					atomicAdd(A.settled_fathers, 1ull);
+				if (left == 0) {
+					if (tid < u) {
+						const int16_t job = S.fr[l1 + 1 + tid];
+						A.child_job[c0 + tid] = job;
+						A.child_job[c0 + u + tid] = job;
 					}
 					__syncthreads();
-					if (active)
-						job_pairs(S, my_s * len / NS, (my_s + 1) * len / NS, my_j, xs, accB, accE);
+					continue;
 				}
+				acc = Sl::none();
 			}
-			__syncthreads(); // the reduction overwrites the X rows
-			S.red[2 * tid] = accB;
-			S.red[2 * tid + 1] = accE;
+			// every pair, in chunks
+			for (int p_lo = 0; p_lo < P; p_lo += L.pc) {
+				if (p_lo > 0 || kLearned)
+					__syncthreads(); // the previous chunk (or red) consumed
+				chunk_bounds<kWide, k16>(S, tjT, jobposT, bp, nullptr, p_lo, min(L.pc, P - p_lo),
+				                         !kLearned && p_lo == 0, scan, xs, l1, l2, u, ract, rj, rs,
+				                         NS, acc);
+			}
+			__syncthreads(); // red overwrites the X rows
+			red[tid] = acc;
 			__syncthreads();
 			if (tid < u) {
-				int32_t lbB = S.red[2 * tid], lbE = S.red[2 * tid + 1];
-				for (int s = 1; s < NS; ++s) {
-					lbB = max(lbB, S.red[2 * (s * u32 + tid)]);
-					lbE = max(lbE, S.red[2 * (s * u32 + tid) + 1]);
-				}
+				T s = red[tid];
+				for (int k = 1; k < NS; ++k)
+					s = Sl::vmax(s, red[k * u + tid]);
 				const int16_t job = S.fr[l1 + 1 + tid];
 				A.child_job[c0 + tid] = job;
 				A.child_job[c0 + u + tid] = job;
-				if (!kLearned) {
-					A.child_lb[c0 + tid] = lbB;
-					A.child_lb[c0 + u + tid] = lbE;
-				} else {
-					// settled children keep the bound over the K pairs
-					if (lbB >= thr)
-						A.child_lb[c0 + tid] = lbB;
-					else
-						S.list[atomicAdd(S.cnt, 1)] = int16_t(tid);
-					if (lbE >= thr)
-						A.child_lb[c0 + u + tid] = lbE;
-					else
-						S.list[atomicAdd(S.cnt, 1)] = int16_t(u + tid);
-				}
-			}
-			if (kLearned) {
-				__syncthreads();
-				const int nu = *S.cnt;
-				if (tid == 0 && 2 * u - nu > 0)
-					atomicAdd(A.early, (unsigned long long)(2 * u - nu));
-				if (tid == 0 && nu == 0 && A.settled_fathers)
-					atomicAdd(A.settled_fathers, 1ull);
-				if (nu > 0) {
-					// the children left: every pair
-					const int nu32 = (nu + 31) & ~31, NS2 = kFamThreads / nu32;
-					const int ci = tid % nu32, cs = tid / nu32;
-					const bool act2 = cs < NS2 && ci < nu;
-					const int c = act2 ? S.list[ci] : 0;
-					const bool begin = c < u;
-					const int j = S.fr[l1 + 1 + (begin ? c : c - u)];
-					int32_t acc = kNeg;
-					for (int p_lo = 0; p_lo < P; p_lo += L.pc) {
-						const int len = min(L.pc, P - p_lo);
-						__syncthreads();
-						for (int t = tid; t < len; t += kFamThreads)
-							{
-						if (scan)
-							scan_pair<kWide>(S, tjT, p_lo + t, t, n, P, xs, w0, w1, w2, w3);
-						else
-							walk_pair<kWide>(S, tjT, jobposT, p_lo + t, t, n, P, xs, fj, u);
-					}
-						__syncthreads();
-						if (act2)
-							acc = child_pairs(S, cs * len / NS2, (cs + 1) * len / NS2, j, begin, xs,
-							                  acc);
-					}
-					__syncthreads();
-					S.red[tid] = acc;
-					__syncthreads();
-					if (tid < nu) {
-						int32_t lb = S.red[tid];
-						for (int s = 1; s < NS2; ++s)
-							lb = max(lb, S.red[s * nu32 + tid]);
-						A.child_lb[c0 + S.list[tid]] = lb;
-					}
-				}
+				if (needB)
+					A.child_lb[c0 + tid] = Sl::begin(s);
+				if (needE)
+					A.child_lb[c0 + u + tid] = Sl::end(s);
 			}
 			__syncthreads();
 		} while (0);
@@ -653,7 +665,8 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 
 size_t family_smem(const BoundParams &bp, int smem_kb)
 {
-	return fam_layout(bp.n, bp.m, bp.P, size_t(smem_kb > 0 ? smem_kb : 56) * 1024).bytes;
+	return fam_layout(bp.n, bp.m, bp.P, size_t(smem_kb > 0 ? smem_kb : 56) * 1024, bp.span16 != 0)
+	    .bytes;
 }
 
 cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, const FamilyArgs &A,
@@ -662,11 +675,17 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, cons
 	if (max_fathers <= 0)
 		return cudaSuccess;
 	const size_t budget = size_t(std::min(std::max(smem_kb > 0 ? smem_kb : 56, 16), 220)) * 1024;
-	const FamLayout L = fam_layout(bp.n, bp.m, bp.P, budget);
+	const bool p16 = bp.span16 != 0;
+	const FamLayout L = fam_layout(bp.n, bp.m, bp.P, budget, p16);
 	const bool learned = A.fpairs != nullptr;
 	const bool wide = bp.n > 64;
-	auto kern = learned ? (wide ? family_kernel<true, true> : family_kernel<true, false>)
-	                    : (wide ? family_kernel<false, true> : family_kernel<false, false>);
+	using Kern = void (*)(FamilyArgs, BoundParams, const uint2 *, const uint8_t *, FamLayout);
+	static const Kern kernels[8] = {
+	    family_kernel<false, false, false>, family_kernel<false, false, true>,
+	    family_kernel<false, true, false>,  family_kernel<false, true, true>,
+	    family_kernel<true, false, false>,  family_kernel<true, false, true>,
+	    family_kernel<true, true, false>,   family_kernel<true, true, true>};
+	const Kern kern = kernels[(learned ? 4 : 0) + (wide ? 2 : 0) + (p16 ? 1 : 0)];
 	cudaError_t e = allow_max_dynamic_smem(kern);
 	if (e != cudaSuccess)
 		return e;

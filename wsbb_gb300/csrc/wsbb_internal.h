@@ -69,6 +69,10 @@ struct BoundParams {
 	int n, m, P;
 	int stride; // record stride in bytes
 	int col16;  // 1: every front/back time fits int16 (total work < 32768)
+	// 1: (n + m - 1) * max p <= 65535. Every time a bound of this instance
+	// produces is the length of a staircase path through the machine x job
+	// grid of some permutation (n + m - 1 operations), so it fits uint16.
+	int span16 = 0;
 	// When set, the kernels read the record count from device memory and
 	// the host-side count only sizes the grid (graph-captured launches).
 	const long long *count_dev = nullptr;
