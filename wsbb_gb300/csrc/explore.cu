@@ -224,12 +224,64 @@ struct IntSumOp {
 
 __device__ __forceinline__ bool halted(const ExDev *D) { return D->done || D->error; }
 
+// Exclusive prefix sums over `count` items (one CTA of kSelThreads): item i
+// has value get(i) (a non-negative int); put(i, sum of the items before
+// i). A round stages kScanItems * kSelThreads items in shared memory with
+// coalesced loads, each thread scans kScanItems consecutive ones (row
+// padding of one word per 32 keeps those reads conflict-free), and the
+// results leave with coalesced stores. Returns the total.
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanItems * kSelThreads;
+__device__ __forceinline__ int scan_pad(int i) { return i + (i >> 5); }
+template <typename Get, typename Put>
+__device__ long long cta_scan(long long count, Get get, Put put, long long *s_ll)
+{
+	__shared__ int tile[kScanTile + kScanTile / 32];
+	const int t = threadIdx.x;
+	long long carry = 0;
+	for (long long base = 0; base < count; base += kScanTile) {
+#pragma unroll
+		for (int k = 0; k < kScanItems; ++k) {
+			const int j = k * kSelThreads + t;
+			tile[scan_pad(j)] = base + j < count ? get(base + j) : 0;
+		}
+		__syncthreads();
+		int v[kScanItems];
+		int sum = 0;
+#pragma unroll
+		for (int k = 0; k < kScanItems; ++k) {
+			v[k] = tile[scan_pad(t * kScanItems + k)];
+			sum += v[k];
+		}
+		long long tot;
+		// the prefix inside a round fits int: at most kScanTile items of a
+		// stack block or child count each
+		int run = int(block_excl_scan<kSelThreads>((long long)sum, SumOp(), 0ll, s_ll, &tot));
+#pragma unroll
+		for (int k = 0; k < kScanItems; ++k) {
+			tile[scan_pad(t * kScanItems + k)] = run;
+			run += v[k];
+		}
+		__syncthreads();
+#pragma unroll
+		for (int k = 0; k < kScanItems; ++k) {
+			const int j = k * kSelThreads + t;
+			if (base + j < count)
+				put(base + j, carry + tile[scan_pad(j)]);
+		}
+		carry += tot;
+		__syncthreads(); // the tile is reused
+	}
+	return carry;
+}
+
 // ---- commit: walk down from the top in DFS order -------------------------
 __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 {
 	__shared__ int s_int[32];
 	__shared__ unsigned long long s_cnt[6];
-	__shared__ unsigned long long s_hist[WSBB_MAX_JOBS + 1];
+	// per-iteration depth counts (at most window * n each: 32 bits)
+	__shared__ unsigned s_hist[WSBB_MAX_JOBS + 1];
 	ExDev *D = P.dev;
 	if (halted(D))
 		return;
@@ -318,15 +370,10 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 						}
 					}
 				}
-				// one shared atomic per distinct depth per warp: most entries
-				// of a chunk share a few depths (warps with nothing to add,
-				// past the committed run, skip it)
-				if (__any_sync(0xffffffffu, hkey != 255)) {
-					const unsigned grp = __match_any_sync(0xffffffffu, hkey);
-					const unsigned sum = __reduce_add_sync(grp, hval);
-					if (hkey != 255 && (threadIdx.x & 31) == __ffs(grp) - 1)
-						atomicAdd(&s_hist[hkey], (unsigned long long)sum);
-				}
+				// 32-bit shared atomics (64-bit ones under contention cost
+				// far more than the lanes that collide here)
+				if (hkey != 255)
+					atomicAdd(&s_hist[hkey], hval);
 			}
 		}
 		const int cmin =
@@ -355,7 +402,7 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 		// speculatively built under it is dropped.
 		if (t == 0) {
 			c_pr++;
-			atomicAdd(&s_hist[stopper.depth], 1ull);
+			atomicAdd(&s_hist[stopper.depth], 1u);
 		}
 		top -= 1;
 		while (top >= 0) {
@@ -376,12 +423,16 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 		}
 	}
 
-	atomicAdd(&s_cnt[0], c_br);
-	atomicAdd(&s_cnt[1], c_pr);
-	atomicAdd(&s_cnt[2], c_lf);
-	atomicAdd(&s_cnt[3], c_im);
-	atomicAdd(&s_cnt[4], c_bd);
-	atomicAdd(&s_cnt[5], c_dead);
+	// warp sums first: 1024 threads on one 64-bit shared counter serialise
+	unsigned long long cv[6] = {c_br, c_pr, c_lf, c_im, c_bd, c_dead};
+#pragma unroll
+	for (int q = 0; q < 6; ++q) {
+#pragma unroll
+		for (int d = 16; d > 0; d >>= 1)
+			cv[q] += __shfl_xor_sync(0xffffffffu, cv[q], d);
+		if ((t & 31) == 0)
+			atomicAdd(&s_cnt[q], cv[q]);
+	}
 	__syncthreads();
 	if (t == 0) {
 		D->branched += s_cnt[0];
@@ -513,16 +564,10 @@ __global__ void __launch_bounds__(kSelThreads) select_plan_kernel(ExParams P)
 	ExDev *D = P.dev;
 	if (halted(D))
 		return;
-	long long carry = 0;
-	for (int base = 0; base < P.n_chunks; base += kSelThreads) {
-		const int c = base + threadIdx.x;
-		const long long v = c < P.n_chunks ? P.chunk_cnt[c] : 0;
-		long long tot;
-		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
-		if (c < P.n_chunks)
-			P.chunk_cnt[c] = int(min(carry + ex, (long long)INT_MAX)); // now the chunk base
-		carry += tot;
-	}
+	// each chunk's count becomes the chunk's base
+	const long long carry = cta_scan(
+	    P.n_chunks, [&](long long c) { return P.chunk_cnt[c]; },
+	    [&](long long c, long long v) { P.chunk_cnt[c] = int(min(v, (long long)INT_MAX)); }, s_ll);
 	if (threadIdx.x == 0)
 		D->n_fathers = min(carry, (long long)D->win);
 }
@@ -579,16 +624,9 @@ __global__ void __launch_bounds__(kSelThreads) father_scan_kernel(ExParams P)
 	if (halted(D) || D->n_fathers == 0)
 		return;
 	const long long nf = D->n_fathers;
-	long long carry = 0;
-	for (long long base = 0; base < nf; base += kSelThreads) {
-		const long long f = base + threadIdx.x;
-		const long long v = f < nf ? P.father_children[f] : 0;
-		long long tot;
-		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
-		if (f < nf)
-			P.child_off[f] = carry + ex;
-		carry += tot;
-	}
+	const long long carry = cta_scan(
+	    nf, [&](long long f) { return P.father_children[f]; },
+	    [&](long long f, long long v) { P.child_off[f] = v; }, s_ll);
 	if (threadIdx.x == 0) {
 		P.child_off[nf] = carry;
 		D->n_children = carry;
@@ -743,16 +781,9 @@ __global__ void __launch_bounds__(kSelThreads) kept_scan_kernel(ExParams P)
 	if (halted(D) || D->n_fathers == 0)
 		return;
 	const long long nf = D->n_fathers;
-	long long carry = 0;
-	for (long long base = 0; base < nf; base += kSelThreads) {
-		const long long f = base + threadIdx.x;
-		const long long v = f < nf ? 1 + P.father_kept[f] : 0;
-		long long tot;
-		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
-		if (f < nf)
-			P.kept_before[f] = carry + ex;
-		carry += tot;
-	}
+	const long long carry = cta_scan(
+	    nf, [&](long long f) { return 1 + P.father_kept[f]; },
+	    [&](long long f, long long v) { P.kept_before[f] = v; }, s_ll);
 	if (threadIdx.x == 0) {
 		P.kept_before[nf] = carry;
 		const long long slots = (D->region_len - nf) + carry;
@@ -766,72 +797,99 @@ __global__ void __launch_bounds__(kSelThreads) kept_scan_kernel(ExParams P)
 	}
 }
 
-// Scatter the rewritten region: one warp per region entry. Region entry r
-// has r - fb non-father entries above it (one slot each) and fb father
-// blocks (kept_before[fb] slots), fb = fathers above it.
+// Half q (0-7) of a 16-byte record word set to v.
+__device__ __forceinline__ void set_half(uint4 &w, int q, int16_t v)
+{
+	const int sh = (q & 1) * 16;
+	const uint32_t keep = ~(0xffffu << sh), val = uint32_t(uint16_t(v)) << sh;
+	const int i = q >> 1;
+	w.x = i == 0 ? (w.x & keep) | val : w.x;
+	w.y = i == 1 ? (w.y & keep) | val : w.y;
+	w.z = i == 2 ? (w.z & keep) | val : w.z;
+	w.w = i == 3 ? (w.w & keep) | val : w.w;
+}
+
+// Scatter the rewritten region, one thread per item: items [0, rlen) move
+// region entry r (fathers become BRANCHED markers) and items rlen + f n + k
+// write child k of father f's chosen side when it is still open. Region
+// entry r has r - fb non-father entries above it (one slot each) and fb
+// father blocks (kept_before[fb] slots), fb = fathers above it; a father's
+// open children sit just above its marker, by rank.
 __global__ void emit_kernel(ExParams P)
 {
 	ExDev *D = P.dev;
 	if (halted(D) || D->n_fathers == 0)
 		return;
-	const int lane = threadIdx.x & 31;
-	const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-	const int S = P.stride, n = P.n;
-	const long long rlen = D->region_len;
+	const int S = P.stride, n = P.n, W = S / 16;
+	const long long rlen = D->region_len, nf = D->n_fathers;
 	const long long new_top = D->top - rlen + D->region_slots;
-	for (long long r = warp; r < rlen; r += nwarps) {
-		const int fb = P.fathers_before[r];
-		const long long hi_slot = new_top - ((r - fb) + P.kept_before[fb]);
-		const int f = P.father_of[r];
-		const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
-		for (int c = lane; c < S / 16; c += 32)
-			reinterpret_cast<uint4 *>(P.rec + hi_slot * S)[c] = src[c];
-		if (f < 0) {
-			if (lane == 0)
-				P.meta[hi_slot] = P.tmp_meta[r];
+	const long long items = rlen + nf * n;
+	const long long gsz = (long long)gridDim.x * blockDim.x;
+	for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < items; w += gsz) {
+		if (w < rlen) {
+			const long long r = w;
+			const int fb = P.fathers_before[r];
+			const long long hi_slot = new_top - ((r - fb) + P.kept_before[fb]);
+			const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
+			uint4 *dst = reinterpret_cast<uint4 *>(P.rec + hi_slot * S);
+			for (int c = 0; c < W; ++c)
+				dst[c] = src[c];
+			Meta mm = P.tmp_meta[r];
+			const int f = P.father_of[r];
+			if (f >= 0) {
+				mm.state = ST_BRANCHED;
+				mm.npruned = uint16_t(P.father_npr[f]);
+			}
+			P.meta[hi_slot] = mm;
 			continue;
 		}
+		const long long f = (w - rlen) / n;
+		const int k = int((w - rlen) - f * n);
+		const long long r = P.father_ridx[f];
 		const Meta fm = P.tmp_meta[r];
 		const bool simple = fm.depth == n - 2;
-		const int side_off = P.father_side[f];
-		const long long c0 = P.child_off[f] + side_off;
-		const int16_t *fr16 = reinterpret_cast<const int16_t *>(P.tmp_rec + r * S);
-		const int fl1 = fr16[n], fl2 = fr16[n + 1];
 		const int kept_all = simple ? 2 : int(P.child_off[f + 1] - P.child_off[f]) / 2;
-		const int open = P.father_kept[f];
-		for (int k = lane; k < kept_all; k += 32) {
-			const long long ck = c0 + k;
-			const int rank = P.child_rank[ck];
-			if (rank >= open)
-				continue; // pruned at birth: counted with the marker
-			const long long slot = hi_slot - 1 - rank;
-			// the child record: the father's with the moved job swapped into
-			// its slot and the new cursors (make_children_kernel's rule)
-			uint4 *dst = reinterpret_cast<uint4 *>(P.rec + slot * S);
-			for (int c = 0; c < S / 16; ++c)
-				dst[c] = src[c];
-			int16_t *d16 = reinterpret_cast<int16_t *>(dst);
-			const int indice = fl1 + 1 + k;
-			const int to = (simple || side_off == 0) ? fl1 + 1 : fl2 - 1;
-			d16[indice] = fr16[to];
-			d16[to] = fr16[indice];
-			d16[n] = int16_t(simple ? fl1 + 2 : (side_off == 0 ? fl1 + 1 : fl1));
-			d16[n + 1] = int16_t((simple || side_off == 0) ? fl2 : fl2 - 1);
-			d16[n + 2] = int16_t(simple ? n : fm.depth + 1);
-			Meta cm;
-			cm.lb = P.child_lb[ck];
-			cm.depth = uint8_t(simple ? n : fm.depth + 1);
-			cm.state = simple ? ST_LEAF : ST_UNPROC;
-			cm.npruned = 0;
-			P.meta[slot] = cm;
+		if (k >= kept_all)
+			continue;
+		const int side_off = P.father_side[f];
+		const long long ck = P.child_off[f] + side_off + k;
+		const int rank = P.child_rank[ck];
+		if (rank >= P.father_kept[f])
+			continue; // pruned at birth: counted with the marker
+		const long long slot = new_top - ((r - f) + P.kept_before[f]) - 1 - rank;
+		// the child record: the father's with the moved job swapped into its
+		// slot and the new cursors (make_children_kernel's rule)
+		const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
+		const int16_t *fr16 = reinterpret_cast<const int16_t *>(src);
+		const int fl1 = fr16[n], fl2 = fr16[n + 1];
+		const int indice = fl1 + 1 + k;
+		const int to = (simple || side_off == 0) ? fl1 + 1 : fl2 - 1;
+		const int16_t at_to = fr16[to], at_indice = fr16[indice];
+		const int16_t h_l1 = int16_t(simple ? fl1 + 2 : (side_off == 0 ? fl1 + 1 : fl1));
+		const int16_t h_l2 = int16_t((simple || side_off == 0) ? fl2 : fl2 - 1);
+		const int16_t h_depth = int16_t(simple ? n : fm.depth + 1);
+		uint4 *dst = reinterpret_cast<uint4 *>(P.rec + slot * S);
+		for (int c = 0; c < W; ++c) {
+			uint4 word = src[c];
+			const int lo = 8 * c;
+			if ((indice >> 3) == c)
+				set_half(word, indice - lo, at_to);
+			if ((to >> 3) == c)
+				set_half(word, to - lo, at_indice);
+			if ((n >> 3) == c)
+				set_half(word, n - lo, h_l1);
+			if (((n + 1) >> 3) == c)
+				set_half(word, n + 1 - lo, h_l2);
+			if (((n + 2) >> 3) == c)
+				set_half(word, n + 2 - lo, h_depth);
+			dst[c] = word;
 		}
-		if (lane == 0) {
-			Meta mm = fm;
-			mm.state = ST_BRANCHED;
-			mm.npruned = uint16_t(P.father_npr[f]);
-			P.meta[hi_slot] = mm;
-		}
+		Meta cm;
+		cm.lb = P.child_lb[ck];
+		cm.depth = uint8_t(h_depth);
+		cm.state = simple ? ST_LEAF : ST_UNPROC;
+		cm.npruned = 0;
+		P.meta[slot] = cm;
 	}
 }
 
@@ -1255,7 +1313,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 		return e;
 	choose_kernel<<<grid, 256, 0, s>>>(X.P);
 	kept_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
-	emit_kernel<<<grid, 256, 0, s>>>(X.P);
+	emit_kernel<<<2 * grid, 256, 0, s>>>(X.P); // one thread per item, latency-bound: a full SM
 	finish_iteration_kernel<<<1, 32, 0, s>>>(X.P);
 	return cudaGetLastError();
 }

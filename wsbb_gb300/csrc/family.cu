@@ -101,8 +101,8 @@ struct FamLayout {
 	int xs;   // X row stride in slots (odd: rows of consecutive pairs start in different banks)
 	int pc;   // pairs per chunk
 	int slot; // bytes per X slot (4: packed 16-bit bounds, 8: int32 bounds)
-	size_t off_pairs, off_V, off_W, off_PFR, off_X, off_PI, off_red, off_F, off_G, off_fr,
-	    off_misc, bytes;
+	size_t off_pairs, off_VW, off_PFR, off_X, off_PI, off_red, off_F, off_G, off_fr, off_misc,
+	    bytes;
 };
 
 FamLayout fam_layout(int n, int m, int P, size_t budget, bool pack16)
@@ -115,10 +115,8 @@ FamLayout fam_layout(int n, int m, int P, size_t budget, bool pack16)
 	size_t off = a16(size_t(m) * (n + 1) * 2);
 	L.off_pairs = off;
 	off = a16(off + size_t(P) * 4);
-	L.off_V = off;
-	off = a16(off + size_t(m) * (n + 1) * 4);
-	L.off_W = off;
-	off = a16(off + size_t(m) * (n + 1) * 4);
+	L.off_VW = off;
+	off = a16(off + size_t(m) * (n + 1) * 8);
 	L.off_PFR = off;
 	off = a16(off + size_t(P) * 16);
 	const size_t fixed_after = a16(32 * 4) * 2 + a16(size_t(n + 4) * 2) + 32;
@@ -150,7 +148,11 @@ FamLayout fam_layout(int n, int m, int P, size_t budget, bool pack16)
 
 struct FamSmem {
 	uint16_t *pt;
-	int32_t *pairs, *V, *W, *F, *G;
+	int32_t *pairs, *F, *G;
+	// per (machine k, column j): (V, W) = the front of the BEGIN child that
+	// moves job j and the back of the END child that moves it (column n:
+	// the father's own front, or the heads, and back, or the tails)
+	int2 *VW;
 	int4 *PFR; // per pair: the father's front (m1, m2) and back (m1, m2) times
 	int4 *PI;  // per chunk slot: (m1 (n+1) | m2 (n+1) << 16, A, B, pair)
 	uint8_t *X, *red;
@@ -164,8 +166,7 @@ __device__ __forceinline__ FamSmem carve(uint8_t *smem, const FamLayout &L)
 	FamSmem S;
 	S.pt = reinterpret_cast<uint16_t *>(smem);
 	S.pairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
-	S.V = reinterpret_cast<int32_t *>(smem + L.off_V);
-	S.W = reinterpret_cast<int32_t *>(smem + L.off_W);
+	S.VW = reinterpret_cast<int2 *>(smem + L.off_VW);
 	S.PFR = reinterpret_cast<int4 *>(smem + L.off_PFR);
 	S.X = smem + L.off_X;
 	S.PI = reinterpret_cast<int4 *>(smem + L.off_PI);
@@ -191,6 +192,8 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 {
 	const int ld = n + 1;
 	int2 *pfr = reinterpret_cast<int2 *>(S.PFR);
+	// warp 0 writes the V halves, warp 1 the W halves
+	int32_t *V = reinterpret_cast<int32_t *>(S.VW), *W = V + 1;
 	if (warp == 0) {
 		int32_t Fk = 0;
 		const int nj = l1 + 1;
@@ -206,7 +209,7 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 		}
 		if (lane < m) {
 			S.F[lane] = Fk;
-			S.V[lane * ld + n] = l1 >= 0 ? Fk : heads[lane];
+			V[2 * (lane * ld + n)] = l1 >= 0 ? Fk : heads[lane];
 		}
 		if (leaves_only)
 			return;
@@ -216,12 +219,12 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 			int32_t v = 0;
 			for (int k = 0; k < m; ++k) {
 				v = max(v, S.F[k]) + S.pt[k * ld + j];
-				S.V[k * ld + j] = v;
+				V[2 * (k * ld + j)] = v;
 			}
 		}
 		for (int p = lane; p < P; p += 32) {
 			const int pr = S.pairs[p];
-			pfr[2 * p] = make_int2(S.V[(pr & 0xff) * ld + n], S.V[(pr >> 8) * ld + n]);
+			pfr[2 * p] = make_int2(V[2 * ((pr & 0xff) * ld + n)], V[2 * ((pr >> 8) * ld + n)]);
 		}
 	} else if (warp == 1) {
 		int32_t Gq = 0;
@@ -242,20 +245,20 @@ __device__ __forceinline__ void fronts_and_backs(const FamSmem &S, int warp, int
 			return;
 		__syncwarp();
 		if (lane < m)
-			S.W[lane * ld + n] = l2 < n ? S.G[m - 1 - lane] : tails[lane];
+			W[2 * (lane * ld + n)] = l2 < n ? S.G[m - 1 - lane] : tails[lane];
 		for (int i = lane; i < u; i += 32) {
 			const int j = S.fr[l1 + 1 + i];
 			int32_t g = 0;
 			for (int q = 0; q < m; ++q) {
 				g = max(g, S.G[q]) + S.pt[(m - 1 - q) * ld + j];
-				S.W[(m - 1 - q) * ld + j] = g;
+				W[2 * ((m - 1 - q) * ld + j)] = g;
 			}
 		}
 		__syncwarp();
 		for (int p = lane; p < P; p += 32) {
 			const int pr = S.pairs[p];
-			const int32_t r1 = S.W[(pr & 0xff) * ld + n];
-			pfr[2 * p + 1] = make_int2(l2 < n ? r1 : 0, S.W[(pr >> 8) * ld + n]);
+			const int32_t r1 = W[2 * ((pr & 0xff) * ld + n)];
+			pfr[2 * p + 1] = make_int2(l2 < n ? r1 : 0, W[2 * ((pr >> 8) * ld + n)]);
 		}
 	}
 }
@@ -265,10 +268,23 @@ constexpr int kScanBatch = 8;
 
 // The next free position of a pair's Johnson order (ascending or
 // descending) from its free-position mask (w0: positions 0-63, w1: 64-127);
-// -1 when none is left.
+// -1 when none is left. For n <= 64 the mask is taken as two 32-bit words.
 template <bool kWide>
 __device__ __forceinline__ int next_up(uint64_t &w0, uint64_t &w1)
 {
+	if (!kWide) {
+		uint32_t lo = uint32_t(w0), hi = uint32_t(w0 >> 32);
+		int q = -1;
+		if (lo) {
+			q = __ffs(lo) - 1;
+			lo &= lo - 1;
+		} else if (hi) {
+			q = 31 + __ffs(hi);
+			hi &= hi - 1;
+		}
+		w0 = (uint64_t(hi) << 32) | lo;
+		return q;
+	}
 	if (w0) {
 		const int q = __ffsll((long long)w0) - 1;
 		w0 &= w0 - 1;
@@ -285,6 +301,20 @@ __device__ __forceinline__ int next_up(uint64_t &w0, uint64_t &w1)
 template <bool kWide>
 __device__ __forceinline__ int next_down(uint64_t &w0, uint64_t &w1)
 {
+	if (!kWide) {
+		uint32_t lo = uint32_t(w0), hi = uint32_t(w0 >> 32);
+		int q = -1;
+		if (hi) {
+			const int b = 31 - __clz(hi);
+			hi ^= 1u << b;
+			q = 32 + b;
+		} else if (lo) {
+			q = 31 - __clz(lo);
+			lo ^= 1u << q;
+		}
+		w0 = (uint64_t(hi) << 32) | lo;
+		return q;
+	}
 	if (kWide && w1) {
 		const int q = 63 - __clzll((long long)w1);
 		w1 ^= 1ull << q;
@@ -421,8 +451,8 @@ __device__ __forceinline__ void pair_backward(const FamSmem &S, const uint2 *__r
 		cs = max(cs + a, bs + cj);
 		as += a;
 		bs += b;
-		const int32_t v1 = S.V[row1 + job], v2 = S.V[row2 + job];
-		const int32_t w1 = S.W[row1 + job], w2 = S.W[row2 + job];
+		const int2 e1 = S.VW[row1 + job], e2 = S.VW[row2 + job];
+		const int32_t v1 = e1.x, v2 = e2.x, w1 = e1.y, w2 = e2.y;
 		const int32_t tb = max(max(v2 - b + kb1, v1 + x + fr.w), v1 - a + kb2);
 		const int32_t te = max(max(w2 - b + ke1, w2 + x + fr.x), w1 - a + ke2);
 		xrow[job] = Sl::pack(tb, te);
