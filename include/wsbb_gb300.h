@@ -293,6 +293,10 @@ int wsbb_probe_maxplus_peak(int device, double *ops_per_s);
 
 /* Host helpers (no device work). */
 void wsbb_gen_instance(uint64_t seed, int n, int m, int32_t *p_mxn);
+/* Times uniform in [1, 99] from Taillard's generator and time seed `seed`
+ * (replaces instance_flowshop::unif / generate_instance,
+ * src/instance_flowshop.cpp:74-89, for a given seed), machine-major. */
+int wsbb_taillard_instance(int64_t seed, int n, int m, int32_t *p_mxn);
 int32_t wsbb_neh(const int32_t *p_mxn, int n, int m, int32_t *perm_out);
 /* Seeded random pool in the record format (f in [0, n-3], b in
  * [0, n-3-f]; a share of leaves). */

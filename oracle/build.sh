@@ -42,9 +42,10 @@ done
 
 $CXXREF -c "$HERE/ref_harness/ref_bound.cpp" -o "$OBJ/ref_bound.o"
 $CXXREF -c "$HERE/ref_harness/ref_explore.cpp" -o "$OBJ/ref_explore.o"
+$CXXREF -c "$HERE/ref_harness/ref_gen.cpp" -o "$OBJ/ref_gen.o"
 
-$CXX -shared -o "$HERE/_ref/libref_bound.so" "$OBJ/ref_bound.o" \
-    "$OBJ/bound_flowshop.o" "$OBJ/bound_abstract.o" -lpthread
+$CXX -shared -o "$HERE/_ref/libref_bound.so" "$OBJ/ref_bound.o" "$OBJ/ref_gen.o" \
+    "$OBJ/bound_flowshop.o" "$OBJ/bound_abstract.o" "$OBJ/instance_flowshop.o" -lpthread
 
 $CXX -o "$HERE/_ref/ref_explore" "$OBJ/ref_explore.o" \
     "$OBJ/bound_flowshop.o" "$OBJ/bound_abstract.o" "$OBJ/tree.o" \

@@ -47,6 +47,22 @@ void fs_gen_instance(uint64_t seed, int n, int m, int32_t *p)
 			p[k * n + j] = (int32_t)(1 + sm64_below(&s, 99));
 }
 
+/* Taillard's generator as the reference draws it
+ * (src/instance_flowshop.cpp:74-89): the Lehmer step s <- 16807 s mod
+ * (2^31 - 1), here by direct 64-bit arithmetic (the reference uses Schrage's
+ * decomposition: same values), then a time 1 + floor(q * 99) with the
+ * quotient q = s / (2^31 - 1) taken in single precision, machine-major. */
+void fs_taillard_instance(int64_t seed, int n, int m, int32_t *p)
+{
+	int64_t s = seed;
+	for (int k = 0; k < m; k++)
+		for (int j = 0; j < n; j++) {
+			s = (int64_t)(((uint64_t)s * 16807u) % 2147483647u);
+			float q = (float)s / (float)2147483647;
+			p[k * n + j] = (int32_t)(1 + (int64_t)((double)q * 99.0));
+		}
+}
+
 void fs_random_pool(uint64_t seed, int n, int64_t count, double leaf_share,
                     int32_t *perms, int32_t *l1, int32_t *l2)
 {

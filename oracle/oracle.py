@@ -40,6 +40,7 @@ def lib():
             build()
         L = C.CDLL(_LIB)
         L.fs_gen_instance.argtypes = [C.c_uint64, C.c_int, C.c_int, _i32p]
+        L.fs_taillard_instance.argtypes = [C.c_int64, C.c_int, C.c_int, _i32p]
         L.fs_bound_create.restype = C.c_void_p
         L.fs_bound_create.argtypes = [_i32p, C.c_int, C.c_int]
         L.fs_bound_destroy.argtypes = [C.c_void_p]
@@ -89,6 +90,12 @@ SEL_CB = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_int32), C.c_int, C.c_int, C.POINTER(
 def gen_instance(seed: int, n: int, m: int) -> np.ndarray:
     p = np.empty(m * n, dtype=np.int32)
     lib().fs_gen_instance(seed, n, m, p)
+    return p.reshape(m, n)
+
+
+def taillard_instance(seed: int, n: int, m: int) -> np.ndarray:
+    p = np.empty(m * n, dtype=np.int32)
+    lib().fs_taillard_instance(seed, n, m, p)
     return p.reshape(m, n)
 
 
@@ -230,6 +237,15 @@ class RefBound:
                                     np.ascontiguousarray(l2, dtype=np.int32), len(l1), out,
                                     nthreads)
         return out
+
+
+def ref_taillard_instance(seed: int, n: int, m: int) -> np.ndarray:
+    """The reference's own instance_flowshop::unif stream for `seed`."""
+    R = ref_lib()
+    R.ref_taillard.argtypes = [C.c_long, C.c_int, C.c_int, _i32p]
+    p = np.empty(m * n, dtype=np.int32)
+    R.ref_taillard(seed, n, m, p)
+    return p.reshape(m, n)
 
 
 def ref_explore(p: np.ndarray, ub0: int | None = None, best: int = 99999,

@@ -40,6 +40,28 @@ def test_instances_equal_oracle(W, oracle):
         np.testing.assert_array_equal(W.gen_instance(s, n, m), oracle.gen_instance(s, n, m))
 
 
+def test_taillard_generator_matches_reference_streams(W, oracle):
+    """Taillard's generator: the oracle restatement and the library both
+    reproduce the streams the reference's own instance_flowshop::unif drew
+    (tests/golden/taillard_streams.json), and agree with each other and,
+    where it is built, with the reference on more seeds."""
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "taillard_streams.json")) as f:
+        cases = json.load(f)
+    for c in cases:
+        want = np.array(c["p"], dtype=np.int32).reshape(c["m"], c["n"])
+        np.testing.assert_array_equal(oracle.taillard_instance(c["seed"], c["n"], c["m"]), want)
+        np.testing.assert_array_equal(W.taillard_instance(c["seed"], c["n"], c["m"]), want)
+    rng = np.random.default_rng(5)
+    for seed in [int(x) for x in rng.integers(1, 2**31 - 1, 40)]:
+        a = W.taillard_instance(seed, 30, 7)
+        np.testing.assert_array_equal(a, oracle.taillard_instance(seed, 30, 7))
+        if oracle.have_reference():
+            np.testing.assert_array_equal(a, oracle.ref_taillard_instance(seed, 30, 7))
+    with pytest.raises(ValueError):
+        W.taillard_instance(1, 0, 5)
+
+
 def test_pools_equal_oracle(W, oracle):
     for (s, n, leaf) in [(1, 20, 0.05), (2, 50, 0.0), (9, 100, 0.2)]:
         rec = W.gen_pool(s, n, 777, leaf)

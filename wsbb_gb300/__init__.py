@@ -6,4 +6,5 @@ modules are thin ctypes front ends over wsbb_gb300/_build/libwsbb_gb300.so.
 """
 from ._lib import LIB_PATH, WsbbError, lib  # noqa: F401
 from .bound import (BoundFlowshopGB300, Context, expand_children, gen_instance,  # noqa: F401
-                    gen_pool, neh, node_stride, pack_records, unpack_records)
+                    gen_pool, neh, node_stride, pack_records, taillard_instance,
+                    unpack_records)

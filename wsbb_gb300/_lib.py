@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
         L.wsbb_precompute.argtypes = [vp, C.c_int, C.c_int] + [vp] * 6
         L.wsbb_lb2_eval_host.argtypes = [vp, vp, i64, vp]
         L.wsbb_gen_instance.argtypes = [C.c_uint64, C.c_int, C.c_int, vp]
+        L.wsbb_taillard_instance.argtypes = [C.c_int64, C.c_int, C.c_int, vp]
         L.wsbb_neh.restype = C.c_int32
         L.wsbb_neh.argtypes = [vp, C.c_int, C.c_int, vp]
         L.wsbb_gen_pool.argtypes = [C.c_uint64, C.c_int, i64, C.c_double, vp]

@@ -87,6 +87,16 @@ def gen_instance(seed: int, n: int, m: int) -> np.ndarray:
     return p.reshape(m, n)
 
 
+def taillard_instance(seed: int, n: int, m: int) -> np.ndarray:
+    """Instance from Taillard's generator with time seed `seed`, as the
+    reference's instance_flowshop draws it (machine-major m x n)."""
+    p = np.empty(m * n, dtype=np.int32)
+    rc = lib().wsbb_taillard_instance(int(seed), n, m, p.ctypes.data)
+    if rc != 0:
+        raise ValueError(f"wsbb_taillard_instance: error {rc}")
+    return p.reshape(m, n)
+
+
 def gen_pool(seed: int, n: int, count: int, leaf_share: float = 0.0) -> np.ndarray:
     """Seeded random pool in the record format."""
     rec = np.empty((count, node_stride(n) // 2), dtype=np.int16)

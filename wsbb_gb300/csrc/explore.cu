@@ -727,40 +727,61 @@ __global__ void choose_kernel(ExParams P)
 		if (!simple) {
 			// choise: more children >= best wins; else the larger sum of the
 			// bounds below best; ties go to the END side
-			long long sum[2] = {0, 0};
-			int cut[2] = {0, 0};
+			// (per side, in registers: a runtime-indexed array would live in
+			// local memory)
+			long long sum0 = 0, sum1 = 0;
+			int cut0 = 0, cut1 = 0;
 			for (int k = lane; k < nc; k += 32) {
 				const int lb = P.child_lb[c0 + k];
-				const int sd = k >= kept_all;
-				if (lb >= best)
-					cut[sd]++;
-				else
-					sum[sd] += lb;
+				const bool end_side = k >= kept_all;
+				const bool cut = lb >= best;
+				cut0 += !end_side && cut;
+				cut1 += end_side && cut;
+				sum0 += !end_side && !cut ? lb : 0;
+				sum1 += end_side && !cut ? lb : 0;
 			}
 #pragma unroll
 			for (int d = 16; d > 0; d >>= 1) {
-				sum[0] += __shfl_xor_sync(0xffffffffu, sum[0], d);
-				sum[1] += __shfl_xor_sync(0xffffffffu, sum[1], d);
-				cut[0] += __shfl_xor_sync(0xffffffffu, cut[0], d);
-				cut[1] += __shfl_xor_sync(0xffffffffu, cut[1], d);
+				sum0 += __shfl_xor_sync(0xffffffffu, sum0, d);
+				sum1 += __shfl_xor_sync(0xffffffffu, sum1, d);
+				cut0 += __shfl_xor_sync(0xffffffffu, cut0, d);
+				cut1 += __shfl_xor_sync(0xffffffffu, cut1, d);
 			}
-			const bool begin = cut[0] != cut[1] ? cut[0] > cut[1] : sum[0] > sum[1];
+			const bool begin = cut0 != cut1 ? cut0 > cut1 : sum0 > sum1;
 			side_off = begin ? 0 : kept_all;
 		}
-		// rank 0 = smallest bound, ties to the smaller job (select_worst)
-		int open = 0;
-		for (int k = lane; k < kept_all; k += 32) {
-			const long long ck = c0 + side_off + k;
-			const int lb = P.child_lb[ck];
-			const int job = P.child_job[ck];
-			int rank = 0;
-			for (int q = 0; q < kept_all; ++q) {
-				const int lq = P.child_lb[c0 + side_off + q];
-				const int jq = P.child_job[c0 + side_off + q];
-				rank += (lq < lb) || (lq == lb && jq < job);
+		// rank 0 = smallest bound, ties to the smaller job (select_worst);
+		// child k = lane + 32 i is held by its lane in slot i and the others'
+		// keys arrive by shuffle
+		constexpr int kSlots = (WSBB_MAX_JOBS + 31) / 32;
+		int lbs[kSlots], jbs[kSlots];
+#pragma unroll
+		for (int i = 0; i < kSlots; ++i) {
+			const int k = lane + 32 * i;
+			const bool in = k < kept_all;
+			lbs[i] = in ? P.child_lb[c0 + side_off + k] : INT_MAX;
+			jbs[i] = in ? int(P.child_job[c0 + side_off + k]) : INT_MAX;
+		}
+		int rk[kSlots] = {};
+#pragma unroll
+		for (int j = 0; j < kSlots; ++j) {
+			const int qn = min(32, kept_all - 32 * j); // <= 0: slot j holds none
+			for (int q = 0; q < qn; ++q) {
+				const int lq = __shfl_sync(0xffffffffu, lbs[j], q);
+				const int jq = __shfl_sync(0xffffffffu, jbs[j], q);
+#pragma unroll
+				for (int i = 0; i < kSlots; ++i)
+					rk[i] += (lq < lbs[i]) || (lq == lbs[i] && jq < jbs[i]);
 			}
-			P.child_rank[ck] = rank;
-			open += (simple || lb < ub) ? 1 : 0;
+		}
+		int open = 0;
+#pragma unroll
+		for (int i = 0; i < kSlots; ++i) {
+			const int k = lane + 32 * i;
+			if (k < kept_all) {
+				P.child_rank[c0 + side_off + k] = rk[i];
+				open += (simple || lbs[i] < ub) ? 1 : 0;
+			}
 		}
 #pragma unroll
 		for (int d = 16; d > 0; d >>= 1)

@@ -462,7 +462,7 @@ __device__ __forceinline__ void pair_backward(const FamSmem &S, const uint2 *__r
 
 // Bounds of the father's children over one chunk of pairs (slot t holds
 // pair fp[t] when fp is set, else p_lo + t), folded into `acc` for the
-// calling thread's job column rj and its slice of slots. The front
+// calling thread's job column rj over the slots t = rs (mod NS). The front
 // threads compute the fronts and backs first when `fronts` is set. Called
 // by every thread; X must be free on entry.
 template <bool kWide, bool k16>
@@ -470,7 +470,7 @@ __device__ __forceinline__ void chunk_bounds(const FamSmem &S, const uint2 *__re
                                              const uint8_t *__restrict__ jobposT,
                                              const BoundParams &bp, const int16_t *fp, int p_lo,
                                              int len, bool fronts, bool scan, int xs, int l1,
-                                             int l2, int u, bool ract, int rj, int rlo, int rhi,
+                                             int l2, int u, bool ract, int rj, int rs, int NS,
                                              typename Slot<k16>::T &acc)
 {
 	using Sl = Slot<k16>;
@@ -511,8 +511,7 @@ __device__ __forceinline__ void chunk_bounds(const FamSmem &S, const uint2 *__re
 	__syncthreads();
 	if (ract) {
 		const typename Sl::T *col = reinterpret_cast<const typename Sl::T *>(S.X) + rj;
-		const int lo = rlo * len / rhi, hi = (rlo + 1) * len / rhi;
-		for (int t = lo; t < hi; ++t)
+		for (int t = rs; t < len; t += NS)
 			acc = Sl::vmax(acc, col[t * xs]);
 	}
 }
@@ -607,11 +606,14 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 					atomicOr(&S.mask[S.fr[l1 + 1 + tid] >> 5], 1u << (S.fr[l1 + 1 + tid] & 31));
 				__syncthreads();
 			}
-			// the final sweep: thread (free job tid % u, slice rs) of NS slices
-			const int NS = min(kFamThreads / u, 32);
-			const int rs = tid / u;
+			// the final sweep: thread (free job tid - rs u, slice rs) of NS
+			// slices. tid / u without an integer division: (tid + 1/2) / u
+			// lies at least 1/(2u) >= 1/256 from an integer, far beyond the
+			// float error of a quotient below 256
+			const int rs = int((float(tid) + 0.5f) * __frcp_rn(float(u)));
+			const int NS = min(int((float(kFamThreads) + 0.5f) * __frcp_rn(float(u))), 32);
 			const bool ract = rs < NS;
-			const int rj = ract ? S.fr[l1 + 1 + tid % u] : 0;
+			const int rj = ract ? S.fr[l1 + 1 + (tid - rs * u)] : 0;
 			T acc = Sl::none();
 			int32_t lbB = 0, lbE = 0;
 			bool needB = true, needE = true;

@@ -260,6 +260,31 @@ extern "C" void wsbb_gen_instance(uint64_t seed, int n, int m, int32_t *p)
 			p[k * n + j] = int32_t(1 + g.below(99));
 }
 
+// Taillard's generator (E. Taillard, "Benchmarks for basic scheduling
+// problems", EJOR 64, 1993): the Lehmer sequence seed' = 16807 seed mod
+// (2^31 - 1), computed with Schrage's decomposition (127773 = m div 16807,
+// 2836 = m mod 16807) so that no intermediate leaves 32 bits, and a time
+// low + floor(seed / m * (high - low + 1)). The reference
+// (src/instance_flowshop.cpp:74-82) forms the quotient seed / m in single
+// precision, which this follows so that the streams agree time for time.
+// Times are drawn machine-major (src/instance_flowshop.cpp:84-89).
+extern "C" int wsbb_taillard_instance(int64_t seed, int n, int m, int32_t *p)
+{
+	if (!p || n <= 0 || m <= 0)
+		return WSBB_ERR_ARG;
+	const int64_t mod = 2147483647, mult = 16807, q = 127773, r = 2836;
+	int64_t s = seed;
+	for (int k = 0; k < m; ++k)
+		for (int j = 0; j < n; ++j) {
+			s = mult * (s % q) - (s / q) * r;
+			if (s < 0)
+				s += mod;
+			const double u01 = double(float(s) / float(mod));
+			p[k * n + j] = int32_t(1 + int64_t(u01 * 99.0));
+		}
+	return WSBB_OK;
+}
+
 extern "C" size_t wsbb_node_stride(int n)
 {
 	return (size_t(2 * n + 8) + 15) & ~size_t(15);
