@@ -146,6 +146,13 @@ int wsbb_lb2_eval_host(wsbb_ctx *ctx, const void *host_recs, int64_t count,
 #define WSBB_EXPLORE_CHILD_LB2 2 /* bound each child record on its own (the
                                     per-node LB2 kernel) instead of each
                                     father's children together; same bounds */
+#define WSBB_EXPLORE_RESUME 4    /* continue the context's stopped (or seeded)
+                                    search — its stack, incumbent and
+                                    counters — instead of starting at the
+                                    root; cfg->ub0 may lower the incumbent
+                                    (a cost found elsewhere), and window and
+                                    capacity must be those of the stopped
+                                    search */
 
 typedef struct {
 	int32_t ub0;         /* initial incumbent cost (INT32_MAX: none) */
@@ -193,6 +200,34 @@ typedef struct {
 
 int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
                  void *stream);
+
+/*
+ * Work hand-off between searches (the reference's peers hand each other
+ * node lists, BB_PROBLEM_PACKET, src/work_stealing/node.cpp:524-560 and
+ * 1240-1283).
+ *
+ * wsbb_explore_export takes up to max_count open nodes from the bottom of
+ * the context's stopped search — the shallowest ones, whose subtrees the
+ * search would take last — out of that search and copies their records and
+ * bounds to host memory in stack order (bottom first); *count_out receives
+ * how many. Open nodes the incumbent already prunes are not taken.
+ *
+ * wsbb_explore_seed replaces the context's search state by one whose stack
+ * holds `count` given open nodes (host records of wsbb_node_stride(n) bytes,
+ * recs[0] at the bottom and the last one taken first, with their bounds),
+ * incumbent cfg->ub0 and zero counters; wsbb_explore with
+ * WSBB_EXPLORE_RESUME (and the same window and capacity) runs it. Records
+ * that are not open nodes of this instance are rejected.
+ *
+ * A peer's counters cover the subtrees it explored; they add up across
+ * peers to the whole tree's as long as no node was exported from under a
+ * branched node that the incumbent later prunes (such a node's subtree is
+ * counted as pruned where it was branched).
+ */
+int wsbb_explore_export(wsbb_ctx *ctx, int64_t max_count, void *recs_out, int32_t *lbs_out,
+                        int64_t *count_out, void *stream);
+int wsbb_explore_seed(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const void *recs,
+                      const int32_t *lbs, int64_t count, void *stream);
 
 /*
  * The same search for callers that cannot allocate GPU memory — code that

@@ -72,13 +72,16 @@ namespace {
 
 // CONDEMNED: a marker the incumbent already prunes whose whole subtree is
 // marked DEAD, so commit can count it as pruned without walking the subtree.
+// EXPORTED: an open node handed to another search (wsbb_explore_export);
+// commit passes over it without counting it.
 enum : uint8_t {
 	ST_UNPROC = 0,
 	ST_LEAF = 1,
 	ST_PRUNED = 2,
 	ST_BRANCHED = 3,
 	ST_DEAD = 4,
-	ST_CONDEMNED = 5
+	ST_CONDEMNED = 5,
+	ST_EXPORTED = 6
 };
 
 struct Meta {
@@ -109,6 +112,7 @@ struct ExDev {
 	unsigned long long early;      // children settled by the learned K-pair test
 	unsigned long long settled_fathers; // fathers whose children it settled all
 	long long n_unsettled;         // children left for full LB2 this iteration
+	long long exported;            // nodes the last export took
 	unsigned long long log_count;  // training records written
 	unsigned long long hist[WSBB_MAX_JOBS + 1];
 };
@@ -357,6 +361,8 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 						hval = 1;
 					} else if (e[i].state == ST_DEAD) {
 						c_dead++; // inside a subtree the sequential search prunes
+					} else if (e[i].state == ST_EXPORTED) {
+						// another search took it over
 					} else { // leaf
 						c_lf++;
 						hkey = n;
@@ -953,6 +959,88 @@ __global__ void init_kernel(ExParams P, int ub0, int best, int win_min, int win_
 	}
 }
 
+// A search state whose stack holds `count` given open nodes (records and
+// meta already in place, entry 0 at the bottom).
+__global__ void seed_kernel(ExParams P, long long count, int ub0, int best, int win_min,
+                            int win_max)
+{
+	ExDev *D = P.dev;
+	const int n = P.n, S = P.stride;
+	if (threadIdx.x == 0) {
+		memset(D, 0, sizeof(ExDev));
+		D->top = count - 1;
+		D->done = count == 0;
+		D->ub = ub0;
+		D->best = best;
+		D->win = win_min;
+		D->win_min = win_min;
+		D->win_max = win_max;
+		D->win_cap = win_max;
+	}
+	for (int j = threadIdx.x; j < S / 2; j += blockDim.x)
+		reinterpret_cast<int16_t *>(P.best_rec)[j] = int16_t(j < n ? -1 : 0);
+}
+
+// Continue a stopped search: an incumbent found elsewhere may lower the
+// cost (its permutation stays with whoever found it).
+__global__ void resume_kernel(ExParams P, int ub0, int best)
+{
+	ExDev *D = P.dev;
+	if (threadIdx.x == 0) {
+		D->ub = min(D->ub, ub0);
+		D->best = best;
+		D->done = D->top < 0 ? 1 : 0;
+	}
+}
+
+// Take up to max_count open nodes from the bottom of the stack (one CTA):
+// each is copied to tmp_rec / tmp_meta in stack order and left EXPORTED.
+// Open nodes the incumbent already prunes are not taken.
+__global__ void __launch_bounds__(kSelThreads) export_kernel(ExParams P, long long max_count)
+{
+	__shared__ long long s_ll[32];
+	ExDev *D = P.dev;
+	const long long top = D->top;
+	const int ub = D->ub, S = P.stride, t = threadIdx.x;
+	long long taken = 0;
+	for (long long base = 0; base <= top && taken < max_count; base += kChunk) {
+		// thread t holds entries base + kItems t + i
+		long long cand = 0;
+#pragma unroll
+		for (int i = 0; i < kItems; ++i) {
+			const long long idx = base + (long long)kItems * t + i;
+			if (idx <= top) {
+				const Meta e = P.meta[idx];
+				cand += e.state == ST_UNPROC && e.lb < ub;
+			}
+		}
+		long long tot;
+		long long order = taken + block_excl_scan<kSelThreads>(cand, SumOp(), 0ll, s_ll, &tot);
+#pragma unroll
+		for (int i = 0; i < kItems; ++i) {
+			const long long idx = base + (long long)kItems * t + i;
+			if (idx > top)
+				break;
+			Meta e = P.meta[idx];
+			if (e.state != ST_UNPROC || e.lb >= ub)
+				continue;
+			if (order < max_count) {
+				const uint4 *src = reinterpret_cast<const uint4 *>(P.rec + idx * S);
+				uint4 *dst = reinterpret_cast<uint4 *>(P.tmp_rec + order * S);
+				for (int c = 0; c < S / 16; ++c)
+					dst[c] = src[c];
+				P.tmp_meta[order] = e;
+				e.state = ST_EXPORTED;
+				P.meta[idx] = e;
+			}
+			++order;
+		}
+		taken = min(max_count, taken + tot);
+	}
+	if (t == 0)
+		D->exported = taken;
+}
+
 // ---- learned mode ----------------------------------------------------------
 
 // Features of every father (from the region copy), for the pair selector.
@@ -1380,19 +1468,15 @@ struct SearchMode {
 	int log_stride = 1;
 };
 
-int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, wsbb_stats *st,
-               void *stream_v, long long *logged)
+// Stack capacity and window of a search configuration.
+int search_shape(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, int &window, long long &cap,
+                 long long &region_cap)
 {
 	using namespace wsbb;
-	if (!ctx || !cfg || !st)
-		return WSBB_ERR_ARG;
-	cudaError_t e = cudaSetDevice(ctx->device);
-	if (e != cudaSuccess)
-		return ex_fail(ctx, e, "cudaSetDevice");
 	const int n = ctx->inst.n;
 	const int S = ctx->bp.stride;
-	const int window = cfg->window > 0 ? cfg->window : 16384;
-	long long cap = cfg->capacity;
+	window = cfg->window > 0 ? cfg->window : 16384;
+	cap = cfg->capacity;
 	if (cap <= 0) {
 		// A `window`-wide DFS keeps up to about window * u entries per level
 		// live: 2 * window * n^2 covers it, within half the free memory.
@@ -1405,16 +1489,25 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	}
 	// Scanning past pruned entries to fill the window is cheap next to an
 	// under-filled iteration; the region copy grows with it.
-	const long long region_cap = 16ll * window + 8192;
+	region_cap = 16ll * window + 8192;
 	if (window > (1 << 20) || cap < region_cap)
 		return wsbb_set_error(ctx, WSBB_ERR_ARG, "window / capacity out of range");
+	return WSBB_OK;
+}
 
+// The context's search state for this shape (allocated, or reallocated when
+// the shape changed, which drops any stopped search).
+int search_state(wsbb_ctx *ctx, int window, long long cap, long long region_cap)
+{
+	using namespace wsbb;
+	const int n = ctx->inst.n;
+	const int S = ctx->bp.stride;
 	ExploreState *X = ctx->ex;
 	if (!X || X->cap != cap || X->window != window) {
 		wsbb_explore_release(ctx);
 		X = new ExploreState();
 		X->bytes = search_layout(nullptr, cap, region_cap, window, n, S, X->P);
-		e = cudaMalloc(&X->mem, X->bytes);
+		const cudaError_t e = cudaMalloc(&X->mem, X->bytes);
 		if (e != cudaSuccess) {
 			delete X;
 			return wsbb_set_error(ctx, WSBB_ERR_NOMEM, "search pool allocation failed");
@@ -1428,6 +1521,32 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 		X->child_bp.count_dev = &X->P.dev->n_children;
 		ctx->ex = X;
 	}
+	return WSBB_OK;
+}
+
+int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, wsbb_stats *st,
+               void *stream_v, long long *logged)
+{
+	using namespace wsbb;
+	if (!ctx || !cfg || !st)
+		return WSBB_ERR_ARG;
+	cudaError_t e = cudaSetDevice(ctx->device);
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "cudaSetDevice");
+	const int n = ctx->inst.n;
+	const int S = ctx->bp.stride;
+	int window = 0;
+	long long cap = 0, region_cap = 0;
+	int rc = search_shape(ctx, cfg, window, cap, region_cap);
+	if (rc != WSBB_OK)
+		return rc;
+	const bool resume = (cfg->flags & WSBB_EXPLORE_RESUME) != 0;
+	if (resume && (!ctx->ex || ctx->ex->cap != cap || ctx->ex->window != window))
+		return wsbb_set_error(ctx, WSBB_ERR_ARG,
+		                      "no stopped search of this window and capacity to resume");
+	if ((rc = search_state(ctx, window, cap, region_cap)) != WSBB_OK)
+		return rc;
+	ExploreState *X = ctx->ex;
 	if (M.mode == 1) {
 		int D = 0;
 		wsbb_model_dims(M.model, &D, nullptr, nullptr);
@@ -1460,7 +1579,10 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	// work queued on the legacy default stream
 	if (!stream_v && (e = wait_for_legacy(s)) != cudaSuccess)
 		return ex_fail(ctx, e, "stream ordering");
-	init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window);
+	if (resume)
+		resume_kernel<<<1, 32, 0, s>>>(X->P, cfg->ub0, cfg->best);
+	else
+		init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window);
 	e = cudaGetLastError();
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "search init");
@@ -1564,6 +1686,102 @@ extern "C" int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_sta
                             void *stream)
 {
 	return run_search(ctx, cfg, SearchMode(), st, stream, nullptr);
+}
+
+extern "C" int wsbb_explore_seed(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const void *recs,
+                                 const int32_t *lbs, int64_t count, void *stream)
+{
+	using namespace wsbb;
+	if (!ctx || !cfg || count < 0 || (count > 0 && (!recs || !lbs)))
+		return WSBB_ERR_ARG;
+	cudaError_t e = cudaSetDevice(ctx->device);
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "cudaSetDevice");
+	const int n = ctx->inst.n, S = ctx->bp.stride;
+	int window = 0;
+	long long cap = 0, region_cap = 0;
+	int rc = search_shape(ctx, cfg, window, cap, region_cap);
+	if (rc != WSBB_OK)
+		return rc;
+	if (count > cap - region_cap)
+		return wsbb_set_error(ctx, WSBB_ERR_CAPACITY, "more seed nodes than the stack holds");
+	// records are checked on the host: the search indexes its tables by them
+	const int16_t *r16 = static_cast<const int16_t *>(recs);
+	std::vector<Meta> meta((size_t)count);
+	for (int64_t i = 0; i < count; ++i) {
+		const int16_t *r = r16 + i * (S / 2);
+		const int l1 = r[n], l2 = r[n + 1], depth = r[n + 2];
+		unsigned seen[(WSBB_MAX_JOBS + 31) / 32] = {};
+		bool ok = l1 >= -1 && l2 <= n && l2 - l1 >= 3 && depth == n - (l2 - l1 - 1);
+		for (int j = 0; ok && j < n; ++j) {
+			const int v = r[j];
+			ok = v >= 0 && v < n && !(seen[v >> 5] >> (v & 31) & 1u);
+			if (ok)
+				seen[v >> 5] |= 1u << (v & 31);
+		}
+		if (!ok)
+			return wsbb_set_error(ctx, WSBB_ERR_ARG, "seed record is not an open node");
+		meta[size_t(i)] = Meta{lbs[i], uint8_t(depth), ST_UNPROC, 0};
+	}
+	if ((rc = search_state(ctx, window, cap, region_cap)) != WSBB_OK)
+		return rc;
+	ExploreState *X = ctx->ex;
+	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+	if (count > 0)
+		e = cudaMemcpyAsync(X->P.rec, recs, size_t(count) * S, cudaMemcpyHostToDevice, s);
+	if (e == cudaSuccess && count > 0)
+		e = cudaMemcpyAsync(X->P.meta, meta.data(), size_t(count) * sizeof(Meta),
+		                    cudaMemcpyHostToDevice, s);
+	if (e == cudaSuccess) {
+		seed_kernel<<<1, 128, 0, s>>>(X->P, count, cfg->ub0, cfg->best, window_min_of(window),
+		                              window);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(s); // the host meta buffer goes out of scope
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "search seed");
+	return WSBB_OK;
+}
+
+extern "C" int wsbb_explore_export(wsbb_ctx *ctx, int64_t max_count, void *recs_out,
+                                   int32_t *lbs_out, int64_t *count_out, void *stream)
+{
+	using namespace wsbb;
+	if (!ctx || max_count < 0 || !count_out || (max_count > 0 && (!recs_out || !lbs_out)))
+		return WSBB_ERR_ARG;
+	*count_out = 0;
+	if (!ctx->ex)
+		return wsbb_set_error(ctx, WSBB_ERR_ARG, "no search state to export from");
+	cudaError_t e = cudaSetDevice(ctx->device);
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "cudaSetDevice");
+	ExploreState *X = ctx->ex;
+	const int S = ctx->bp.stride;
+	// the region copy stages the exported nodes
+	const long long take = std::min<long long>(max_count, X->region_cap);
+	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+	export_kernel<<<1, kSelThreads, 0, s>>>(X->P, take);
+	e = cudaGetLastError();
+	long long got = 0;
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(&got, &X->P.dev->exported, sizeof(got), cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(s);
+	std::vector<Meta> meta(size_t(std::max(got, 0ll)));
+	if (e == cudaSuccess && got > 0)
+		e = cudaMemcpyAsync(recs_out, X->P.tmp_rec, size_t(got) * S, cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess && got > 0)
+		e = cudaMemcpyAsync(meta.data(), X->P.tmp_meta, size_t(got) * sizeof(Meta),
+		                    cudaMemcpyDeviceToHost, s);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(s);
+	if (e != cudaSuccess)
+		return ex_fail(ctx, e, "search export");
+	for (long long i = 0; i < got; ++i)
+		lbs_out[i] = meta[size_t(i)].lb;
+	*count_out = got;
+	return WSBB_OK;
 }
 
 extern "C" int wsbb_explore_learned(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,

@@ -13,7 +13,7 @@ import math
 import numpy as np
 
 from ._lib import WsbbError, lib
-from .bound import Context
+from .bound import Context, node_stride
 
 INT32_MAX = 2**31 - 1
 MAX_JOBS = 128
@@ -38,6 +38,7 @@ class ExploreStats(C.Structure):
 
 NO_GRAPH = 1
 CHILD_LB2 = 2  # bound every child record on its own instead of per father (same bounds)
+RESUME = 4     # continue the context's stopped or seeded search
 
 
 def coverage(hist, n: int) -> int:
@@ -45,24 +46,73 @@ def coverage(hist, n: int) -> int:
     return sum(int(hist[d]) * math.factorial(n - d) for d in range(n + 1))
 
 
+def _cfg(ub0, best, window, graph_iters, capacity, max_iters, flags, family_smem_kb,
+         max_bounded) -> ExploreCfg:
+    return ExploreCfg(INT32_MAX if ub0 is None else int(ub0), int(best), int(window),
+                      int(graph_iters), int(capacity), int(max_iters), flags,
+                      int(family_smem_kb), int(max_bounded))
+
+
 def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int = 0,
             graph_iters: int = 0, capacity: int = 0, max_iters: int = 0, graph: bool = True,
             stream: int = 0, child_lb2: bool = False, family_smem_kb: int = 0,
-            max_bounded: int = 0) -> dict:
+            max_bounded: int = 0, resume: bool = False) -> dict:
     """The exact GPU search. `child_lb2` bounds each child record on its own
     with the per-node LB2 kernel (the reference GPU kernel's form) instead of
-    each father's children together; bounds and tree are the same."""
+    each father's children together; bounds and tree are the same.
+    `resume` continues the context's stopped or seeded search (same window
+    and capacity; `ub0` may lower its incumbent); its counters are
+    cumulative since the start or the seed."""
     L = lib()
     L.wsbb_explore.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
-    flags = (0 if graph else NO_GRAPH) | (CHILD_LB2 if child_lb2 else 0)
-    cfg = ExploreCfg(INT32_MAX if ub0 is None else int(ub0), int(best), int(window),
-                     int(graph_iters), int(capacity), int(max_iters), flags,
-                     int(family_smem_kb), int(max_bounded))
+    flags = (0 if graph else NO_GRAPH) | (CHILD_LB2 if child_lb2 else 0) | \
+        (RESUME if resume else 0)
+    cfg = _cfg(ub0, best, window, graph_iters, capacity, max_iters, flags, family_smem_kb,
+               max_bounded)
     st = ExploreStats()
     rc = L.wsbb_explore(ctx.h, C.byref(cfg), C.byref(st), stream or None)
     if rc != 0:
         raise WsbbError(rc, L.wsbb_last_error(ctx.h).decode())
-    n = ctx.n
+    return stats_dict(st, ctx.n)
+
+
+def explore_seed(ctx: Context, records: np.ndarray, lbs, ub0: int | None = None,
+                 best: int = 99999, window: int = 0, capacity: int = 0,
+                 stream: int = 0) -> None:
+    """Replace the context's search state by one whose stack holds the
+    given open nodes (records[0] at the bottom, the last taken first) with
+    their bounds; `explore(..., resume=True)` runs it."""
+    L = lib()
+    L.wsbb_explore_seed.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_int64, C.c_void_p]
+    rec = np.ascontiguousarray(records, dtype=np.int16)
+    lb = np.ascontiguousarray(lbs, dtype=np.int32)
+    if rec.ndim != 2 or rec.shape[1] * 2 != node_stride(ctx.n) or len(lb) != len(rec):
+        raise ValueError("records must be (count, wsbb_node_stride(n) / 2) int16 with one bound each")
+    cfg = _cfg(ub0, best, window, 0, capacity, 0, 0, 0, 0)
+    rc = L.wsbb_explore_seed(ctx.h, C.byref(cfg), rec.ctypes.data, lb.ctypes.data, len(rec),
+                             stream or None)
+    if rc != 0:
+        raise WsbbError(rc, L.wsbb_last_error(ctx.h).decode())
+
+
+def explore_export(ctx: Context, max_count: int, stream: int = 0):
+    """Take up to `max_count` open nodes from the bottom of the context's
+    stopped search: (records, bounds) in stack order, bottom first."""
+    L = lib()
+    L.wsbb_explore_export.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p]
+    rec = np.zeros((max(max_count, 0), node_stride(ctx.n) // 2), dtype=np.int16)
+    lb = np.zeros(max(max_count, 0), dtype=np.int32)
+    got = C.c_int64(0)
+    rc = L.wsbb_explore_export(ctx.h, int(max_count), rec.ctypes.data, lb.ctypes.data,
+                               C.byref(got), stream or None)
+    if rc != 0:
+        raise WsbbError(rc, L.wsbb_last_error(ctx.h).decode())
+    return rec[:got.value].copy(), lb[:got.value].copy()
+
+
+def stats_dict(st: ExploreStats, n: int) -> dict:
     return {"branched": st.branched, "pruned": st.pruned, "leaves": st.leaves,
             "improved": st.improved, "bounded": st.bounded, "evaluated": st.evaluated,
             "discarded": st.discarded, "iterations": st.iterations,
