@@ -58,8 +58,8 @@ S_N, S_M, S_NODES, S_ITER_CAP = 50, 20, 250_000_000, 20_000
 MODEL = os.path.join(ROOT, "wsbb_gb300", "models", f"selector_n{S_N}_m{S_M}.npz")
 TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost", "coverage")
 # kernels per search iteration (family bounds): commit, doom, select x3,
-# father scan, region copy, family bounds, choose, kept scan, emit, finish
-KERNELS_PER_ITER = 12
+# region copy, family bounds, choose, kept scan, emit, finish
+KERNELS_PER_ITER = 11
 
 POOL_N, POOL_M, POOL, POOL_SEEDS, LEAF_SHARE = 20, 20, 1 << 20, 10, 0.02
 PROOF_N, PROOF_M, PROOF_SEEDS = 50, 10, (0, 1, 2, 3, 4)

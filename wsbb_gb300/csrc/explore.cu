@@ -29,10 +29,10 @@
 //                       them whenever it reaches them, since the incumbent
 //                       never increases — so their subtrees are marked dead
 //                       and never expanded further.
-//   select (3 kernels)  Count the unprocessed nodes of the top region per
-//                       chunk (bound >= incumbent prunes them, final), plan
-//                       the first `window` of them, and mark those fathers.
-//   father scan         Child offsets of the fathers.
+//   select (3 kernels)  Count the unprocessed nodes of the top region and
+//                       their children per chunk (bound >= incumbent prunes
+//                       them, final), plan the first `window` of them, and
+//                       mark those fathers with their first child's offset.
 //   make_children       Copy the rewrite region aside and write every
 //                       father's 2u children (both sides) or 2 leaves as pool
 //                       records (create_raw_problem3,
@@ -125,10 +125,10 @@ struct ExParams {
 	Meta *tmp_meta;           // [region_cap]
 	int *fathers_before;      // [region_cap] fathers above each region entry
 	int *father_of;           // [region_cap] father ordinal or -1
-	int *chunk_cnt;           // [n_chunks] candidates per select chunk
+	long long *chunk_cnt;     // [n_chunks] candidates << kKidBits | their children, per
+	                          // select chunk (then the chunk's base of both)
 	long long *father_ridx;   // [window] region index of each father
 	long long *child_off;     // [window + 1] first child record of each father
-	int *father_children;     // [window] child records of each father
 	int *father_side;         // [window] offset of the chosen side in its children
 	int *father_kept;         // [window] chosen children still open
 	int *father_npr;          // [window] chosen children pruned at birth
@@ -162,6 +162,11 @@ constexpr int kChunk = kItems * kSelThreads;
 // Select chunks: one 256-thread CTA scans kSelChunk entries.
 constexpr int kSelCtaThreads = 256;
 constexpr int kSelChunk = kItems * kSelCtaThreads;
+// Select counts candidates and their children in one 64-bit sum: children
+// in the low kKidBits bits (at most 2^24 region entries x 256 children),
+// candidates above.
+constexpr int kKidBits = 36;
+constexpr long long kKidMask = (1ll << kKidBits) - 1;
 
 __device__ __forceinline__ int children_of_depth(int depth, int n)
 {
@@ -535,15 +540,16 @@ __global__ void doom_kernel(ExParams P)
 // entry r being stack entry top - r.
 __global__ void __launch_bounds__(kSelCtaThreads) select_count_kernel(ExParams P)
 {
-	__shared__ int s_int[32];
+	__shared__ long long s_ll[32];
 	ExDev *D = P.dev;
 	if (halted(D))
 		return;
 	const long long top = D->top;
 	const int ub = D->ub;
 	const long long scan_len = min(top + 1, P.region_cap);
+	const int n = P.n;
 	for (int c = blockIdx.x; c < P.n_chunks; c += gridDim.x) {
-		int cand = 0;
+		long long cand = 0;
 #pragma unroll
 		for (int i = 0; i < kItems; ++i) {
 			const long long r = (long long)c * kSelChunk + kItems * threadIdx.x + i;
@@ -555,10 +561,10 @@ __global__ void __launch_bounds__(kSelCtaThreads) select_count_kernel(ExParams P
 				if (e.lb >= ub)
 					P.meta[idx].state = ST_PRUNED; // final: the incumbent only decreases
 				else
-					cand++;
+					cand += (1ll << kKidBits) + children_of_depth(e.depth, n);
 			}
 		}
-		const int total = block_reduce<kSelCtaThreads>(cand, IntSumOp(), 0, s_int);
+		const long long total = block_reduce<kSelCtaThreads>(cand, SumOp(), 0ll, s_ll);
 		if (threadIdx.x == 0)
 			P.chunk_cnt[c] = total;
 	}
@@ -570,17 +576,25 @@ __global__ void __launch_bounds__(kSelThreads) select_plan_kernel(ExParams P)
 	ExDev *D = P.dev;
 	if (halted(D))
 		return;
-	// each chunk's count becomes the chunk's base
-	const long long carry = cta_scan(
-	    P.n_chunks, [&](long long c) { return P.chunk_cnt[c]; },
-	    [&](long long c, long long v) { P.chunk_cnt[c] = int(min(v, (long long)INT_MAX)); }, s_ll);
+	// each chunk's counts become the chunk's bases (both fields at once:
+	// neither sum carries into the other)
+	long long carry = 0;
+	for (int base = 0; base < P.n_chunks; base += kSelThreads) {
+		const int c = base + threadIdx.x;
+		const long long v = c < P.n_chunks ? P.chunk_cnt[c] : 0;
+		long long tot;
+		const long long ex = block_excl_scan<kSelThreads>(v, SumOp(), 0ll, s_ll, &tot);
+		if (c < P.n_chunks)
+			P.chunk_cnt[c] = carry + ex;
+		carry += tot;
+	}
 	if (threadIdx.x == 0)
-		D->n_fathers = min(carry, (long long)D->win);
+		D->n_fathers = min(carry >> kKidBits, (long long)D->win);
 }
 
 __global__ void __launch_bounds__(kSelCtaThreads) select_write_kernel(ExParams P)
 {
-	__shared__ int s_int[32];
+	__shared__ long long s_ll[32];
 	ExDev *D = P.dev;
 	if (halted(D))
 		return;
@@ -590,18 +604,20 @@ __global__ void __launch_bounds__(kSelCtaThreads) select_write_kernel(ExParams P
 	const long long scan_len = min(top + 1, P.region_cap);
 	for (int c = blockIdx.x; c < P.n_chunks; c += gridDim.x) {
 		const long long chunk_base = P.chunk_cnt[c];
-		if ((long long)c * kSelChunk >= scan_len || chunk_base >= nf)
+		if ((long long)c * kSelChunk >= scan_len || (chunk_base >> kKidBits) >= nf)
 			continue; // past the region (uniform per CTA)
 		Meta e[kItems];
-		int cand = 0;
+		long long cand = 0;
 #pragma unroll
 		for (int i = 0; i < kItems; ++i) {
 			const long long r = (long long)c * kSelChunk + kItems * threadIdx.x + i;
 			e[i] = r < scan_len ? P.meta[top - r] : Meta{0, 0, ST_DEAD, 0};
-			cand += e[i].state == ST_UNPROC;
+			if (e[i].state == ST_UNPROC)
+				cand += (1ll << kKidBits) + children_of_depth(e[i].depth, n);
 		}
-		long long order = chunk_base + block_excl_scan<kSelCtaThreads>(cand, IntSumOp(), 0, s_int,
-		                                                                (int *)nullptr);
+		const long long ex = chunk_base + block_excl_scan<kSelCtaThreads>(cand, SumOp(), 0ll, s_ll,
+		                                                                   (long long *)nullptr);
+		long long order = ex >> kKidBits, kid = ex & kKidMask;
 #pragma unroll
 		for (int i = 0; i < kItems; ++i) {
 			const long long r = (long long)c * kSelChunk + kItems * threadIdx.x + i;
@@ -610,34 +626,24 @@ __global__ void __launch_bounds__(kSelCtaThreads) select_write_kernel(ExParams P
 			const bool take = e[i].state == ST_UNPROC && order < nf;
 			P.fathers_before[r] = int(min(order, nf));
 			P.father_of[r] = take ? int(order) : -1;
+			if (e[i].state != ST_UNPROC)
+				continue;
+			const int kids = children_of_depth(e[i].depth, n);
 			if (take) {
+				// the father's first child: children of the fathers before it
 				P.father_ridx[order] = r;
-				P.father_children[order] = children_of_depth(e[i].depth, n);
-				if (order == nf - 1)
+				P.child_off[order] = kid;
+				if (order == nf - 1) {
+					P.child_off[nf] = kid + kids;
 					D->region_len = r + 1;
+					D->n_children = kid + kids;
+					D->evaluated += (unsigned long long)(kid + kids);
+					D->scanned += (unsigned long long)(r + 1);
+				}
 			}
-			if (e[i].state == ST_UNPROC)
-				order++;
+			order++;
+			kid += kids;
 		}
-	}
-}
-
-// Child offsets of the fathers (one CTA).
-__global__ void __launch_bounds__(kSelThreads) father_scan_kernel(ExParams P)
-{
-	__shared__ long long s_ll[32];
-	ExDev *D = P.dev;
-	if (halted(D) || D->n_fathers == 0)
-		return;
-	const long long nf = D->n_fathers;
-	const long long carry = cta_scan(
-	    nf, [&](long long f) { return P.father_children[f]; },
-	    [&](long long f, long long v) { P.child_off[f] = v; }, s_ll);
-	if (threadIdx.x == 0) {
-		P.child_off[nf] = carry;
-		D->n_children = carry;
-		D->evaluated += (unsigned long long)carry;
-		D->scanned += (unsigned long long)D->region_len;
 	}
 }
 
@@ -769,15 +775,24 @@ __global__ void choose_kernel(ExParams P)
 			jbs[i] = in ? int(P.child_job[c0 + side_off + k]) : INT_MAX;
 		}
 		int rk[kSlots] = {};
+		if (kept_all <= 32) {
+			// one slot: the common case
+			for (int q = 0; q < kept_all; ++q) {
+				const int lq = __shfl_sync(0xffffffffu, lbs[0], q);
+				const int jq = __shfl_sync(0xffffffffu, jbs[0], q);
+				rk[0] += (lq < lbs[0]) || (lq == lbs[0] && jq < jbs[0]);
+			}
+		} else {
 #pragma unroll
-		for (int j = 0; j < kSlots; ++j) {
-			const int qn = min(32, kept_all - 32 * j); // <= 0: slot j holds none
-			for (int q = 0; q < qn; ++q) {
-				const int lq = __shfl_sync(0xffffffffu, lbs[j], q);
-				const int jq = __shfl_sync(0xffffffffu, jbs[j], q);
+			for (int j = 0; j < kSlots; ++j) {
+				const int qn = min(32, kept_all - 32 * j); // <= 0: slot j holds none
+				for (int q = 0; q < qn; ++q) {
+					const int lq = __shfl_sync(0xffffffffu, lbs[j], q);
+					const int jq = __shfl_sync(0xffffffffu, jbs[j], q);
 #pragma unroll
-				for (int i = 0; i < kSlots; ++i)
-					rk[i] += (lq < lbs[i]) || (lq == lbs[i] && jq < jbs[i]);
+					for (int i = 0; i < kSlots; ++i)
+						rk[i] += (lq < lbs[i]) || (lq == lbs[i] && jq < jbs[i]);
+				}
 			}
 		}
 		int open = 0;
@@ -836,87 +851,106 @@ __device__ __forceinline__ void set_half(uint4 &w, int q, int16_t v)
 	w.w = i == 3 ? (w.w & keep) | val : w.w;
 }
 
-// Scatter the rewritten region, one thread per item: items [0, rlen) move
-// region entry r (fathers become BRANCHED markers) and items rlen + f n + k
-// write child k of father f's chosen side when it is still open. Region
-// entry r has r - fb non-father entries above it (one slot each) and fb
-// father blocks (kept_before[fb] slots), fb = fathers above it; a father's
-// open children sit just above its marker, by rank.
-__global__ void emit_kernel(ExParams P)
+// Scatter the rewritten region. Work items, grid-strided: first one thread
+// per 16-byte word of every region entry (region entry r moves to its new
+// slot; fathers become BRANCHED markers), then one warp per father, which
+// writes the father's open children — contiguous slots just above its
+// marker, by rank — as one coalesced run of words. Region entry r has
+// r - fb non-father entries above it (one slot each) and fb father blocks
+// (kept_before[fb] slots), fb = fathers above it.
+constexpr int kEmitThreads = 256;
+__global__ void __launch_bounds__(kEmitThreads) emit_kernel(ExParams P)
 {
+	__shared__ uint8_t s_inv[kEmitThreads / 32][WSBB_MAX_JOBS]; // per warp: rank -> child
 	ExDev *D = P.dev;
 	if (halted(D) || D->n_fathers == 0)
 		return;
 	const int S = P.stride, n = P.n, W = S / 16;
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
 	const long long rlen = D->region_len, nf = D->n_fathers;
 	const long long new_top = D->top - rlen + D->region_slots;
-	const long long items = rlen + nf * n;
+	const long long words = rlen * W;
+	const long long part2 = (words + 31) & ~31ll; // fathers start on a warp boundary
+	const long long items = part2 + nf * 32;
 	const long long gsz = (long long)gridDim.x * blockDim.x;
-	for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < items; w += gsz) {
-		if (w < rlen) {
-			const long long r = w;
+	for (long long w0 = (long long)blockIdx.x * blockDim.x; w0 < items; w0 += gsz) {
+		const long long w = w0 + threadIdx.x;
+		const long long wbase = w0 + (threadIdx.x & ~31); // the warp's first item
+		if (wbase >= items)
+			continue; // past the last father (warp-uniform)
+		if (wbase < part2) {
+			if (w >= words)
+				continue;
+			const long long r = w / W;
+			const int c = int(w - r * W);
 			const int fb = P.fathers_before[r];
 			const long long hi_slot = new_top - ((r - fb) + P.kept_before[fb]);
-			const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
-			uint4 *dst = reinterpret_cast<uint4 *>(P.rec + hi_slot * S);
-			for (int c = 0; c < W; ++c)
-				dst[c] = src[c];
-			Meta mm = P.tmp_meta[r];
-			const int f = P.father_of[r];
-			if (f >= 0) {
-				mm.state = ST_BRANCHED;
-				mm.npruned = uint16_t(P.father_npr[f]);
+			reinterpret_cast<uint4 *>(P.rec + hi_slot * S)[c] =
+			    reinterpret_cast<const uint4 *>(P.tmp_rec + r * S)[c];
+			if (c == 0) {
+				Meta mm = P.tmp_meta[r];
+				const int f = P.father_of[r];
+				if (f >= 0) {
+					mm.state = ST_BRANCHED;
+					mm.npruned = uint16_t(P.father_npr[f]);
+				}
+				P.meta[hi_slot] = mm;
 			}
-			P.meta[hi_slot] = mm;
 			continue;
 		}
-		const long long f = (w - rlen) / n;
-		const int k = int((w - rlen) - f * n);
+		const long long f = (wbase - part2) >> 5; // < nf
 		const long long r = P.father_ridx[f];
 		const Meta fm = P.tmp_meta[r];
 		const bool simple = fm.depth == n - 2;
 		const int kept_all = simple ? 2 : int(P.child_off[f + 1] - P.child_off[f]) / 2;
-		if (k >= kept_all)
-			continue;
 		const int side_off = P.father_side[f];
-		const long long ck = P.child_off[f] + side_off + k;
-		const int rank = P.child_rank[ck];
-		if (rank >= P.father_kept[f])
-			continue; // pruned at birth: counted with the marker
-		const long long slot = new_top - ((r - f) + P.kept_before[f]) - 1 - rank;
-		// the child record: the father's with the moved job swapped into its
-		// slot and the new cursors (make_children_kernel's rule)
+		const long long c0 = P.child_off[f] + side_off;
+		const int open = P.father_kept[f];
+		for (int k = lane; k < kept_all; k += 32) {
+			const int rank = P.child_rank[c0 + k];
+			if (rank < open)
+				s_inv[wib][rank] = uint8_t(k);
+		}
+		__syncwarp();
+		// the child of rank q sits at slot hi_slot - 1 - q: the run starts
+		// at the highest rank
+		const long long lo_slot = new_top - ((r - f) + P.kept_before[f]) - open;
 		const uint4 *src = reinterpret_cast<const uint4 *>(P.tmp_rec + r * S);
 		const int16_t *fr16 = reinterpret_cast<const int16_t *>(src);
 		const int fl1 = fr16[n], fl2 = fr16[n + 1];
-		const int indice = fl1 + 1 + k;
 		const int to = (simple || side_off == 0) ? fl1 + 1 : fl2 - 1;
-		const int16_t at_to = fr16[to], at_indice = fr16[indice];
+		const int16_t at_to = fr16[to];
 		const int16_t h_l1 = int16_t(simple ? fl1 + 2 : (side_off == 0 ? fl1 + 1 : fl1));
 		const int16_t h_l2 = int16_t((simple || side_off == 0) ? fl2 : fl2 - 1);
 		const int16_t h_depth = int16_t(simple ? n : fm.depth + 1);
-		uint4 *dst = reinterpret_cast<uint4 *>(P.rec + slot * S);
-		for (int c = 0; c < W; ++c) {
+		uint4 *dst = reinterpret_cast<uint4 *>(P.rec + lo_slot * S);
+		for (int wi = lane; wi < open * W; wi += 32) {
+			const int j = wi / W, c = wi - j * W; // run record j holds rank open - 1 - j
+			const int k = s_inv[wib][open - 1 - j];
+			const int indice = fl1 + 1 + k;
 			uint4 word = src[c];
 			const int lo = 8 * c;
 			if ((indice >> 3) == c)
 				set_half(word, indice - lo, at_to);
 			if ((to >> 3) == c)
-				set_half(word, to - lo, at_indice);
+				set_half(word, to - lo, fr16[indice]);
 			if ((n >> 3) == c)
 				set_half(word, n - lo, h_l1);
 			if (((n + 1) >> 3) == c)
 				set_half(word, n + 1 - lo, h_l2);
 			if (((n + 2) >> 3) == c)
 				set_half(word, n + 2 - lo, h_depth);
-			dst[c] = word;
+			dst[wi] = word;
+			if (c == 0) {
+				Meta cm;
+				cm.lb = P.child_lb[c0 + k];
+				cm.depth = uint8_t(h_depth);
+				cm.state = simple ? ST_LEAF : ST_UNPROC;
+				cm.npruned = 0;
+				P.meta[lo_slot + j] = cm;
+			}
 		}
-		Meta cm;
-		cm.lb = P.child_lb[ck];
-		cm.depth = uint8_t(h_depth);
-		cm.state = simple ? ST_LEAF : ST_UNPROC;
-		cm.npruned = 0;
-		P.meta[slot] = cm;
+		__syncwarp(); // s_inv is reused by the warp's next father
 	}
 }
 
@@ -1265,10 +1299,9 @@ size_t search_layout(uint8_t *base, long long cap, long long region_cap, int win
 	P.tmp_meta = reinterpret_cast<Meta *>(take(size_t(region_cap) * sizeof(Meta)));
 	P.fathers_before = reinterpret_cast<int *>(take(size_t(region_cap) * 4));
 	P.father_of = reinterpret_cast<int *>(take(size_t(region_cap) * 4));
-	P.chunk_cnt = reinterpret_cast<int *>(take(size_t(n_chunks) * 4));
+	P.chunk_cnt = reinterpret_cast<long long *>(take(size_t(n_chunks) * 8));
 	P.father_ridx = reinterpret_cast<long long *>(take(size_t(window) * 8));
 	P.child_off = reinterpret_cast<long long *>(take(size_t(window + 1) * 8));
-	P.father_children = reinterpret_cast<int *>(take(size_t(window) * 4));
 	P.father_side = reinterpret_cast<int *>(take(size_t(window) * 4));
 	P.father_kept = reinterpret_cast<int *>(take(size_t(window) * 4));
 	P.father_npr = reinterpret_cast<int *>(take(size_t(window) * 4));
@@ -1353,7 +1386,6 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 	select_count_kernel<<<sel_grid, kSelCtaThreads, 0, s>>>(X.P);
 	select_plan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	select_write_kernel<<<sel_grid, kSelCtaThreads, 0, s>>>(X.P);
-	father_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
 	make_children_kernel<<<grid, 256, 0, s>>>(X.P, X.mode == 2 || X.child_lb2);
 	cudaError_t e = cudaSuccess;
 	if (X.mode == 1) {
@@ -1422,7 +1454,7 @@ cudaError_t enqueue_iteration(wsbb_ctx *ctx, ExploreState &X, cudaStream_t s)
 		return e;
 	choose_kernel<<<grid, 256, 0, s>>>(X.P);
 	kept_scan_kernel<<<1, kSelThreads, 0, s>>>(X.P);
-	emit_kernel<<<2 * grid, 256, 0, s>>>(X.P); // one thread per item, latency-bound: a full SM
+	emit_kernel<<<2 * grid, kEmitThreads, 0, s>>>(X.P);
 	finish_iteration_kernel<<<1, 32, 0, s>>>(X.P);
 	return cudaGetLastError();
 }
