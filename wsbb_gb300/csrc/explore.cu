@@ -482,12 +482,17 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 // ---- doom: stop expanding under markers the new incumbent condemns ----------
 // One warp walks the top region in DFS order carrying one value: the depth
 // of the condemned marker whose subtree it is inside (or none). An entry at
-// that depth or shallower ends the subtree; entries inside it are marked
-// dead so select never expands them. A marker outside any such subtree
-// whose bound is not below the incumbent opens one. The marker itself is
-// left as it is: commit prunes it when it reaches the top (the sequential
-// search prunes it on take, the incumbent never increases) and drops its
-// whole subtree by depth, including any part beyond this walk.
+// that depth or shallower ends the subtree (a subtree seen to its end
+// settles its marker as CONDEMNED); entries inside it are marked dead so
+// select never expands them. A marker outside any such subtree whose bound
+// is not below the incumbent opens one. A marker whose subtree runs past
+// the walk is left as it is: commit prunes it when it reaches the top (the
+// sequential search prunes it on take, the incumbent never increases) and
+// drops its whole subtree by depth.
+// The walk takes 32 entries per step: the lane that closes the open subtree
+// and the next marker that opens one are each found with one ballot, so a
+// step costs a few instructions per subtree event instead of a pass per
+// entry.
 __global__ void doom_kernel(ExParams P)
 {
 	ExDev *D = P.dev;
@@ -497,41 +502,48 @@ __global__ void doom_kernel(ExParams P)
 	const long long top = D->top;
 	const int ub = D->ub;
 	const long long stop = max(-1ll, top - P.region_cap);
-	int dd = INT_MAX;         // depth of the open condemned subtree's marker
+	int dd = -1;              // depth of the open condemned subtree's marker (-1: none)
 	long long dd_at = -1;     // its stack index
 	for (long long base = top; base > stop; base -= 32) {
 		const long long idx = base - lane;
+		const bool valid = idx > stop;
 		Meta e = {0, 0, ST_DEAD, 0};
-		if (idx > stop)
+		if (valid)
 			e = P.meta[idx];
-		int new_state = -1;
-		for (int k = 0; k < 32; ++k) {
-			const int depth = __shfl_sync(0xffffffffu, int(e.depth), k);
-			const int state = __shfl_sync(0xffffffffu, int(e.state), k);
-			const int lb = __shfl_sync(0xffffffffu, e.lb, k);
-			if (base - k <= stop)
-				break;
-			int ns = -1;
-			if (depth <= dd) {
-				// a condemned subtree seen to its end: settle its marker
-				if (dd != INT_MAX && lane == 0)
-					P.meta[dd_at].state = ST_CONDEMNED;
-				dd = INT_MAX;
-				if (state == ST_BRANCHED && lb >= ub) {
-					dd = depth;
-					dd_at = base - k;
+		const int depth = e.depth;
+		const unsigned condemned =
+		    __ballot_sync(0xffffffffu, valid && e.state == ST_BRANCHED && e.lb >= ub);
+		unsigned dead = 0;
+		int from = 0; // lanes before `from` are settled for this step
+		for (;;) {
+			const unsigned rest = from >= 32 ? 0u : (0xffffffffu << from);
+			if (dd >= 0) {
+				const unsigned closer = __ballot_sync(0xffffffffu, valid && depth <= dd) & rest;
+				if (!closer) {
+					dead |= __ballot_sync(0xffffffffu, valid) & rest;
+					break; // the subtree goes on past this step
 				}
-			} else {
-				ns = ST_DEAD;
+				const int c = __ffs(closer) - 1;
+				dead |= rest & ~(0xffffffffu << c); // lanes [from, c)
+				if (lane == 0)
+					P.meta[dd_at].state = ST_CONDEMNED;
+				dd = -1;
+				from = c; // the closing entry may open a subtree itself
+				continue;
 			}
-			if (lane == k)
-				new_state = ns;
+			const unsigned opener = condemned & rest;
+			if (!opener)
+				break;
+			const int o = __ffs(opener) - 1;
+			dd = __shfl_sync(0xffffffffu, depth, o);
+			dd_at = base - o;
+			from = o + 1;
 		}
-		if (new_state >= 0 && idx > stop)
-			P.meta[idx].state = uint8_t(new_state);
+		if (valid && ((dead >> lane) & 1u))
+			P.meta[idx].state = ST_DEAD;
 	}
 	// a subtree that runs to the stack bottom also ended inside the walk
-	if (dd != INT_MAX && stop < 0 && lane == 0)
+	if (dd >= 0 && stop < 0 && lane == 0)
 		P.meta[dd_at].state = ST_CONDEMNED;
 }
 
