@@ -34,7 +34,8 @@ class CpuEngine:
 
     def _stats(self):
         return dict(self.c, status=1 if self.stack else 0, best_cost=min(self.ub, self.best_cost),
-                    best_perm=self.best_perm.copy(), coverage=self.cov)
+                    best_perm=self.best_perm.copy(), perm_cost=self.best_cost,
+                    coverage=self.cov)
 
     def start_root(self, ub, budget):
         self._reset(ub)
@@ -142,22 +143,28 @@ def test_two_gloo_peers_find_the_optimum_and_cover_the_tree(at_optimum):
     (_, c0, p0, t0, cov0, s0, r0, n0, k0), (_, c1, p1, t1, cov1, s1, r1, n1, k1) = res
     assert c0 == c1 == seq["best_cost"]
     assert t0 == t1 and cov0 == cov1 == math.factorial(n)     # every subtree exactly once
+    from wsbb_gb300.peers import makespan
+    if p0 is not None:
+        assert makespan(p, np.array(p0)) == c0
     assert n0 == n1 and s0 + s1 > 0 and s0 + s1 == r0 + r1   # work moved, none lost
     assert t0["branched"] == k0["branched"] + k1["branched"]
     if at_optimum:
         assert p0 is None and p1 is None                    # nothing below the optimum
     else:
         assert p0 == p1
-        assert W_makespan(p, p0) == seq["best_cost"]
 
 
-def W_makespan(p, perm):
-    m, n = p.shape
-    t = np.zeros(m + 1, dtype=np.int64)
-    for j in perm:
-        for k in range(m):
-            t[k + 1] = max(t[k + 1], t[k]) + p[k, j]
-    return int(t[m])
+def test_makespan_equals_oracle():
+    import wsbb_gb300 as W
+    from oracle import oracle
+    from wsbb_gb300.peers import makespan
+    rng = np.random.default_rng(9)
+    for n, m in [(9, 3), (20, 20), (50, 10)]:
+        p = W.gen_instance(n + m, n, m)
+        b = oracle.Bound(p)
+        for _ in range(5):
+            perm = rng.permutation(n)
+            assert makespan(p, perm) == b.makespan(perm)
 
 
 def test_three_local_peers_and_termination():
@@ -183,6 +190,7 @@ def test_three_local_peers_and_termination():
     assert {o.total_coverage for o in out} == {math.factorial(n)}
     assert sum(o.received for o in out) == sum(o.sent for o in out) > 0
     assert len({o.rounds for o in out}) == 1            # all stopped at the same round
+    assert all(o.complete for o in out)
     assert all(o.counters["branched"] > 0 for o in out)  # every peer worked
     assert out[0].best_perm.tolist() == out[2].best_perm.tolist()
 

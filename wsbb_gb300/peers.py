@@ -114,6 +114,22 @@ class LocalTransport:
 
 
 # --------------------------------------------------------------------- engine
+#
+# An engine searches on one peer. Its results are dicts with the counters of
+# COUNTERS, "coverage", "status" (0: its search is complete), "best_cost"
+# (its incumbent, which another peer may have lowered) and "best_perm" /
+# "perm_cost": the best permutation it found itself and that permutation's
+# makespan (perm[0] < 0 and INT32_MAX when it found none).
+
+
+def makespan(p: np.ndarray, perm) -> int:
+    """Makespan of a full permutation (machine-major times p)."""
+    t = np.zeros(p.shape[0], dtype=np.int64)
+    for j in perm:
+        t[0] += p[0, j]
+        for k in range(1, p.shape[0]):
+            t[k] = max(t[k], t[k - 1]) + p[k, j]
+    return int(t[-1])
 
 class GpuEngine:
     """The library's search on one context, as a peer's engine. Its unit of
@@ -129,10 +145,23 @@ class GpuEngine:
         # the iteration budget is checked between graph launches of
         # graph_iters iterations
         self.run_kw = dict(family_smem_kb=family_smem_kb, graph_iters=graph_iters)
+        self._perm_key, self._perm_cost = None, INT32_MAX
+
+    def _own(self, st: dict) -> dict:
+        perm = st["best_perm"]
+        if perm[0] < 0:
+            st["perm_cost"] = INT32_MAX
+        else:
+            key = perm.tobytes()
+            if key != self._perm_key:
+                self._perm_key, self._perm_cost = key, makespan(self.ctx.p, perm)
+            st["perm_cost"] = self._perm_cost
+        return st
 
     def start_root(self, ub: int, budget: int) -> dict:
         from .explorer import explore
-        return explore(self.ctx, ub0=ub, max_iters=budget, **self.run_kw, **self.kw)
+        return self._own(explore(self.ctx, ub0=ub, max_iters=budget, **self.run_kw,
+                                 **self.kw))
 
     def seed(self, records: np.ndarray, lbs: np.ndarray, ub: int) -> None:
         from .explorer import explore_seed
@@ -140,8 +169,8 @@ class GpuEngine:
 
     def run(self, ub: int, budget: int) -> dict:
         from .explorer import explore
-        return explore(self.ctx, ub0=ub, resume=True, max_iters=budget, **self.run_kw,
-                       **self.kw)
+        return self._own(explore(self.ctx, ub0=ub, resume=True, max_iters=budget,
+                                 **self.run_kw, **self.kw))
 
     def export(self, max_count: int):
         from .explorer import explore_export
@@ -161,6 +190,7 @@ class PeerResult:
     received: int = 0          # nodes taken from other peers
     total: dict = field(default_factory=dict)  # all peers' counters summed
     total_coverage: int = 0
+    complete: bool = False     # every peer idle (False: max_rounds ran out)
 
 
 def peer_search(engine, transport, n: int, ub0: int | None = None, budget: int | None = None,
@@ -199,13 +229,14 @@ def peer_search(engine, transport, n: int, ub0: int | None = None, budget: int |
         if busy:
             st = engine.run(ub, budget)
             busy = st["status"] != 0
-        if st is not None and st["best_cost"] < own_cost and st["best_perm"][0] >= 0:
-            own_cost, own_perm = int(st["best_cost"]), st["best_perm"].copy()
+        if st is not None and st["perm_cost"] < own_cost:
+            own_cost, own_perm = int(st["perm_cost"]), st["best_perm"].copy()
         mine = min(ub, int(st["best_cost"]) if st is not None else INT32_MAX)
         views = transport.allgather([mine, 0 if busy else 1])
         ub = min(v[0] for v in views)
         idle = [r for r in range(world) if views[r][1]]
         if len(idle) == world:
+            res.complete = True
             break
         donors = [r for r in range(world) if not views[r][1]]
         # receiver i (in rank order) is served by donor i mod len(donors)
