@@ -246,7 +246,9 @@ int wsbb_explore_seed(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const void *re
  * nodes as fit; a configuration that does not fit is rejected with
  * WSBB_ERR_CAPACITY before anything runs, and a search that outgrows the
  * capacity stops with WSBB_ERR_CAPACITY. Iterations are launched one by one
- * (cfg->flags and cfg->graph_iters only set how often the host polls).
+ * (cfg->flags and cfg->graph_iters only set how often the host polls;
+ * WSBB_EXPLORE_RESUME is rejected: the array keeps no search between
+ * calls).
  *
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call

@@ -69,6 +69,10 @@ def test_noalloc_rejects_what_does_not_fit(mods):
                 capacity=1 << 30)
     assert rc == -6
     assert b"MiB" in L.wsbb_last_error(ctx.h)
+    # the array keeps no search between calls: nothing to resume
+    cfg = E.ExploreCfg(INT32_MAX, 99999, 64, 4, 0, 0, E.RESUME, 0)
+    assert L.wsbb_explore_noalloc(ctx.h, C.byref(cfg), C.byref(E.ExploreStats()), None) != 0
+    assert b"resume" in L.wsbb_last_error(ctx.h)
     # and the entry point still works afterwards
     rc, got = run(L, "wsbb_explore_noalloc", ctx, E, INT32_MAX, 99999, window=64)
     assert rc == 0 and got.status == 0

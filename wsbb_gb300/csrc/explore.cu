@@ -1905,6 +1905,9 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	using namespace wsbb;
 	if (!ctx || !cfg || !st)
 		return WSBB_ERR_ARG;
+	// the shared array holds no search between calls
+	if (cfg->flags & WSBB_EXPLORE_RESUME)
+		return wsbb_set_error(ctx, WSBB_ERR_ARG, "the no-alloc search cannot resume");
 	cudaError_t e = cudaSetDevice(ctx->device);
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "cudaSetDevice");
