@@ -104,3 +104,14 @@ def test_work_packet_layout_and_round_trip():
     assert np.array_equal(be2, be) and np.array_equal(rk2, ranks)
     with pytest.raises(ValueError):
         F.unpack_work(data[:-4], n)
+
+
+def test_empty_packet():
+    """A peer with nothing to hand off sends an empty payload."""
+    import wsbb_gb300 as W
+    from wsbb_gb300 import formats
+    n = 7
+    empty = np.zeros((0, W.node_stride(n) // 2), np.int16)
+    assert formats.pack_work(empty, n, np.zeros(0, np.int32), max_nbjobs=n) == b""
+    rec, lbs, be, ranks = formats.unpack_work(b"", n, max_nbjobs=n)
+    assert rec.shape == (0, W.node_stride(n) // 2) and len(lbs) == 0

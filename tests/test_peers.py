@@ -154,6 +154,62 @@ def test_two_gloo_peers_find_the_optimum_and_cover_the_tree(at_optimum):
         assert p0 == p1
 
 
+def test_final_permutation_is_the_winners():
+    """A peer whose incumbent another peer lowered still holds its own older,
+    costlier permutation; the permutation returned is the one of the final
+    cost (scripted engines: peer 0 keeps a permutation of cost 120 and runs
+    once more after peer 1 found one of cost 100)."""
+    import wsbb_gb300 as W
+    from wsbb_gb300 import peers
+
+    def st(ub, status, own_cost, perm):
+        return dict({k: 0 for k in peers.COUNTERS}, status=status, coverage=0,
+                    best_cost=min(ub, own_cost), best_perm=np.array(perm, dtype=np.int32),
+                    perm_cost=own_cost)
+
+    class First:   # busy for three rounds, permutation [2, 1, 0] of cost 120
+        default_budget = 1
+        calls = 0
+
+        def start_root(self, ub, budget):
+            return st(ub, 1, 120, [2, 1, 0])
+
+        def run(self, ub, budget):
+            self.calls += 1
+            return st(ub, 1 if self.calls < 3 else 0, 120, [2, 1, 0])
+
+        def export(self, k):
+            if self.calls == 1:
+                return W.pack_records(np.array([[0, 1, 2]]), [-1], [3]), np.array([50], np.int32)
+            return np.zeros((0, W.node_stride(3) // 2), np.int16), np.zeros(0, np.int32)
+
+    class Second:  # finds [0, 1, 2] of cost 100 in the work it is handed
+        default_budget = 1
+
+        def seed(self, recs, lbs, ub):
+            assert recs[:, :3].tolist() == [[0, 1, 2]] and lbs.tolist() == [50]
+
+        def run(self, ub, budget):
+            return st(ub, 0, 100, [0, 1, 2])
+
+    hub = peers.LocalHub(2)
+    out = [None, None]
+
+    def run(r, eng):
+        out[r] = peers.peer_search(eng, peers.LocalTransport(hub, r), 3)
+
+    th = [threading.Thread(target=run, args=(0, First())),
+          threading.Thread(target=run, args=(1, Second()))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join(timeout=60)
+    assert out[0].complete and out[1].complete
+    assert out[0].best_cost == out[1].best_cost == 100
+    assert out[0].best_perm.tolist() == out[1].best_perm.tolist() == [0, 1, 2]
+    assert out[0].sent == out[1].received == 1
+
+
 def test_makespan_equals_oracle():
     import wsbb_gb300 as W
     from oracle import oracle

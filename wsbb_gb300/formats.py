@@ -112,10 +112,12 @@ def pack_work(records: np.ndarray, n: int, lbs, begin_end=None, ranks=None,
     """BB_PROBLEM_PACKET payload of library records (int16 rows of
     wsbb_node_stride(n)/2) with their bounds; begin_end and ranks (count x
     (MAX_NBJOBS + 1)) default to zeros."""
-    rec = np.asarray(records).reshape(len(records), -1)
-    count = len(rec)
     if n > max_nbjobs:
         raise ValueError("n exceeds MAX_NBJOBS of the packet format")
+    if len(records) == 0:
+        return b""  # nothing to hand off
+    rec = np.asarray(records).reshape(len(records), -1)
+    count = len(rec)
     out = np.zeros((count, packet_ints(max_nbjobs)), dtype="<i4")
     out[:, :n] = rec[:, :n]
     k = max_nbjobs

@@ -85,11 +85,14 @@ class TorchTransport:
 
 
 class LocalHub:
-    """Shared state of in-process peers (one thread each)."""
+    """Shared state of in-process peers (one thread each). A peer that stops
+    without reaching a meeting point breaks the others' waits after
+    `timeout` seconds instead of leaving them blocked."""
 
-    def __init__(self, world: int):
+    def __init__(self, world: int, timeout: float = 600.0):
         self.world = world
-        self.barrier = threading.Barrier(world)
+        self.timeout = timeout
+        self.barrier = threading.Barrier(world, timeout=timeout)
         self.slots: list = [None] * world
         self.boxes = {(s, d): queue.Queue() for s in range(world) for d in range(world)}
 
@@ -110,7 +113,7 @@ class LocalTransport:
         self.hub.boxes[(self.rank, dst)].put(bytes(data))
 
     def recv(self, src: int) -> bytes:
-        return self.hub.boxes[(src, self.rank)].get(timeout=600)
+        return self.hub.boxes[(src, self.rank)].get(timeout=self.hub.timeout)
 
 
 # --------------------------------------------------------------------- engine
