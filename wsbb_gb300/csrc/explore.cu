@@ -221,14 +221,8 @@ __device__ T block_reduce(T v, Op op, T identity, T *scratch)
 struct MinOp {
 	__device__ int operator()(int a, int b) const { return a < b ? a : b; }
 };
-struct MaxOp {
-	__device__ int operator()(int a, int b) const { return a > b ? a : b; }
-};
 struct SumOp {
 	__device__ long long operator()(long long a, long long b) const { return a + b; }
-};
-struct IntSumOp {
-	__device__ int operator()(int a, int b) const { return a + b; }
 };
 
 __device__ __forceinline__ bool halted(const ExDev *D) { return D->done || D->error; }
