@@ -165,6 +165,24 @@ def test_learned_search_keeps_the_tree(env):
         assert got[k] == want[k], k
 
 
+def test_training_gains_early_settles(env):
+    """What training gains over the method without it: the same network at
+    its seeded initial weights ranks pairs too, and settles fewer children
+    with its K pairs than after training; both leave the tree unchanged."""
+    torch, W, E, Lr = env
+    trained, _, _, _ = trained_model(torch, W, Lr, 20, 10, seeds=range(100, 103), epochs=3)
+    start = Lr.Model(20, 10, seed=11)          # trained_model's initial weights
+    p = W.gen_instance(0, 20, 10)
+    ctx = W.Context(p)
+    ub, _ = W.neh(p)
+    for K in (4, 8):
+        a = Lr.explore_learned(ctx, trained, K, ub0=ub, best=ub, window=2048, child_lb2=True)
+        b = Lr.explore_learned(ctx, start, K, ub0=ub, best=ub, window=2048, child_lb2=True)
+        for k in ("branched", "pruned", "bounded", "best_cost"):
+            assert a[k] == b[k], (K, k)
+        assert a["early"] > b["early"], (K, a["early"], b["early"])
+
+
 def test_model_rejects_mismatched_instance(env):
     torch, W, E, Lr = env
     model = Lr.Model(20, 10)
