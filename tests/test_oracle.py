@@ -4,6 +4,8 @@ bound_pools.npz and explore.json were produced by the reference's compiled
 bound_flowshop and CPU search (tests/golden/make_golden.py), so these tests
 pin the oracle before anything else is checked against it.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -109,3 +111,31 @@ def test_reference_harness_live(oracle):
     perms, l1, l2 = oracle.random_pool(5, 9, 500, 0.1)
     np.testing.assert_array_equal(oracle.Bound(p).eval_batch(perms, l1, l2),
                                   oracle.RefBound(p).eval_batch(perms, l1, l2))
+
+
+@pytest.mark.skipif("not __import__('oracle.oracle', fromlist=['x']).have_reference()")
+def test_oracle_matches_the_reference_on_a_sweep(oracle):
+    """Where the reference is built: searches over sizes n = 8..16, m = 2..8,
+    with no incumbent, the NEH incumbent, and best = the NEH cost — every
+    counter, the optimum, its permutation and the coverage equal the
+    reference's own run; and bounds of random pools up to n = 40."""
+    for s, n, m in [(1, 8, 3), (2, 10, 4), (3, 12, 5), (4, 14, 3), (5, 11, 6), (6, 16, 4),
+                    (7, 9, 8), (8, 13, 2)]:
+        p = oracle.gen_instance(s, n, m)
+        ub, _ = oracle.neh(p)
+        for ub0, best in ((None, 99999), (ub, 99999), (ub, ub)):
+            r = oracle.ref_explore(p, ub0=ub0, best=best)
+            rc, st, perm = oracle.Bound(p).explore(ub0=ub0, best=best)
+            assert rc == 0
+            tag = (s, n, m, ub0, best)
+            for k in ("branched", "pruned", "leaves", "improved", "bounded"):
+                assert st[k] == r[k], (tag, k)
+            assert st["best_cost"] == r["optimum"], tag
+            assert st["coverage"] == int(r["coverage"]) == math.factorial(n), tag
+            if st["improved"]:
+                assert list(perm) == list(r["perm"]), tag
+    for s, n, m in [(11, 25, 5), (12, 33, 7), (13, 40, 12)]:
+        p = oracle.gen_instance(s, n, m)
+        perms, l1, l2 = oracle.random_pool(s, n, 400, 0.1)
+        np.testing.assert_array_equal(oracle.Bound(p).eval_batch(perms, l1, l2),
+                                      oracle.RefBound(p).eval_batch(perms, l1, l2))
