@@ -196,6 +196,18 @@ typedef struct {
 	                            all (family bounds) */
 	int64_t d2h_bytes;  /* bytes the search copied device -> host (its state
 	                       between graph launches, the incumbent) */
+	/* Exact prefix of a stopped search. Children whose bound the incumbent
+	 * already reaches when they are generated are counted (pruned,
+	 * depth_hist) when their father is, but the sequential search takes
+	 * them after the subtrees of their open siblings. `pending` of them are
+	 * still ahead of the sequential search where this one stopped
+	 * (pending_hist: by their depth), so the sequential search's counters
+	 * after exactly `takes` takes (nodes popped: branched + pruned + leaves
+	 * - pending) are these counters with pruned - pending and depth_hist -
+	 * pending_hist. Both are 0 once the search completes. */
+	int64_t takes;
+	int64_t pending;
+	uint32_t pending_hist[WSBB_MAX_JOBS + 1];
 } wsbb_stats;
 
 int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
@@ -242,20 +254,26 @@ int wsbb_explore_seed(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const void *re
  * which every GPU that loads the library holds until the process exits.
  * The context must exist already (wsbb_ctx_create allocates the instance
  * tables). Limits: the stack capacity and window are derived from the
- * fixed size — cfg->window 0 means 1024, cfg->capacity 0 means as many
- * nodes as fit; a configuration that does not fit is rejected with
- * WSBB_ERR_CAPACITY before anything runs, and a search that outgrows the
- * capacity stops with WSBB_ERR_CAPACITY. Iterations are launched one by one
- * (cfg->flags and cfg->graph_iters only set how often the host polls;
- * WSBB_EXPLORE_RESUME is rejected: the array keeps no search between
- * calls).
+ * fixed size — cfg->window 0 means the widest of 1024, 512, ..., 64 that
+ * leaves the stack room for 8 iterations of that many fathers (n = 20:
+ * window 1024, about 397k stack nodes; n = 50: 256, about 178k; n = 100:
+ * 64, about 99k), cfg->capacity 0 means as many nodes as fit; a
+ * configuration that does not fit is rejected with WSBB_ERR_CAPACITY
+ * before anything runs, and a search that outgrows the capacity stops with
+ * WSBB_ERR_CAPACITY (the context and the entry point stay usable).
+ * Iterations are launched one by one (cfg->flags and cfg->graph_iters only
+ * set how often the host polls; WSBB_EXPLORE_RESUME is rejected: the array
+ * keeps no search between calls). With a NULL stream it follows the rule
+ * above: it runs on the context's stream after the work already queued on
+ * the legacy default stream (through an event made with the context).
  *
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture. All calls share the one array and the search
- * re-initialises what it reads, so consecutive calls are independent, but
- * calls that overlap on the GPU (from two threads or two streams) race on
- * the array and must be serialised by the caller.
+ * Every call looks up the array's device address (cudaGetSymbolAddress)
+ * with the context's device current; the first such lookup on a device may
+ * load the library's device code, so make the first call before any stream
+ * capture. All calls share the one array and the search re-initialises
+ * what it reads, so consecutive calls are independent, but calls that
+ * overlap on the GPU (from two threads or two streams) race on the array
+ * and must be serialised by the caller.
  */
 #define WSBB_NOALLOC_SCRATCH_BYTES (24u << 20)
 int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,

@@ -643,36 +643,20 @@ static void sort_worst_first(ex_node *v, int cnt)
 
 static void add_coverage(fs_stats *st, int n, int depth)
 {
-	/* weights::depths[d] = (n-d)! for d <= n-1, 1 for d = n (weights.cpp) */
-	unsigned __int128 w = 1;
-	for (int k = 2; k <= n - depth; k++)
-		w *= (unsigned __int128)k;
-	unsigned __int128 c = ((unsigned __int128)st->coverage_hi << 64) |
-	                      st->coverage_lo;
-	c += w;
-	st->coverage_lo = (uint64_t)c;
-	st->coverage_hi = (uint64_t)(c >> 64);
+	/* weights::depths[d] = (n-d)! (weights.cpp), summed by the caller */
+	(void)n;
+	st->depth_hist[depth]++;
 }
 
-int fs_explore(const fs_bound *b, int32_t ub0, int32_t best, int64_t node_cap,
-               fs_stats *st, int32_t *best_perm, fs_log_cb log_cb,
-               fs_pair_sel_cb pair_sel, void *user)
+/* The take loop of explorer::_explore_cpu over a stack that already holds
+ * the starting nodes (the root, or seeded open nodes); frees the stack. */
+static int explore_core(const fs_bound *b, ex_stack S, int32_t ub0, int32_t best,
+                        int64_t node_cap, fs_stats *st, int32_t *best_perm,
+                        fs_log_cb log_cb, fs_pair_sel_cb pair_sel, void *user)
 {
 	int n = b->n;
 	memset(st, 0, sizeof(*st));
 	int32_t ub = ub0; /* the incumbent list's minimum; INT32_MAX = empty */
-	ex_stack S = {0, 0, 0};
-	ex_node root;
-	memset(&root, 0, sizeof(root));
-	for (int j = 0; j < n; j++)
-		root.perm[j] = j;
-	root.l1 = -1;
-	root.l2 = (int16_t)n;
-	root.depth = 0;
-	root.lb = 0;
-	root.job = -1;
-	if (st_push(&S, &root))
-		return -2;
 	ex_node *kids = (ex_node *)malloc(sizeof(ex_node) * 2 * n);
 	int32_t sel[FS_MAX_MACHINES * FS_MAX_MACHINES];
 	int64_t takes = 0;
@@ -775,4 +759,47 @@ done:
 	free(kids);
 	free(S.v);
 	return rc;
+}
+
+int fs_explore(const fs_bound *b, int32_t ub0, int32_t best, int64_t node_cap,
+               fs_stats *st, int32_t *best_perm, fs_log_cb log_cb,
+               fs_pair_sel_cb pair_sel, void *user)
+{
+	int n = b->n;
+	ex_stack S = {0, 0, 0};
+	ex_node root;
+	memset(&root, 0, sizeof(root));
+	for (int j = 0; j < n; j++)
+		root.perm[j] = j;
+	root.l1 = -1;
+	root.l2 = (int16_t)n;
+	root.depth = 0;
+	root.lb = 0;
+	root.job = -1;
+	if (st_push(&S, &root))
+		return -2;
+	return explore_core(b, S, ub0, best, node_cap, st, best_perm, log_cb, pair_sel, user);
+}
+
+int fs_explore_seeded(const fs_bound *b, const int32_t *perms, const int32_t *l1,
+                      const int32_t *l2, const int32_t *lbs, int64_t count, int32_t ub0,
+                      int32_t best, int64_t node_cap, fs_stats *st, int32_t *best_perm)
+{
+	int n = b->n;
+	ex_stack S = {0, 0, 0};
+	for (int64_t i = 0; i < count; i++) {
+		ex_node x;
+		memset(&x, 0, sizeof(x));
+		memcpy(x.perm, perms + i * n, sizeof(int32_t) * n);
+		x.l1 = (int16_t)l1[i];
+		x.l2 = (int16_t)l2[i];
+		x.depth = (int16_t)(n - (l2[i] - l1[i] - 1));
+		x.lb = lbs[i];
+		x.job = -1;
+		if (st_push(&S, &x)) {
+			free(S.v);
+			return -2;
+		}
+	}
+	return explore_core(b, S, ub0, best, node_cap, st, best_perm, NULL, NULL, NULL);
 }

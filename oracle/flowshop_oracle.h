@@ -82,8 +82,10 @@ typedef struct {
 	int64_t early_exits;    /* children settled by the pair-subset test */
 	int32_t best_cost;      /* final incumbent (INT32_MAX if none) */
 	int32_t pad;
-	uint64_t coverage_lo;   /* sum of (n-depth)! over pruned + leaves, 128-bit */
-	uint64_t coverage_hi;
+	/* pruned nodes and leaves taken, per depth: the coverage (the sum of
+	 * (n - depth)! over them, weights.cpp) is formed from it exactly by the
+	 * caller, since it exceeds 128 bits from n = 35 on */
+	uint64_t depth_hist[FS_MAX_JOBS + 1];
 } fs_stats;
 
 /* Exhaustive begin-end DFS with the reference's semantics.
@@ -104,6 +106,13 @@ typedef int (*fs_pair_sel_cb)(const int32_t *perm, int l1, int l2,
 int fs_explore(const fs_bound *b, int32_t ub0, int32_t best, int64_t node_cap,
                fs_stats *stats, int32_t *best_perm, fs_log_cb log_cb,
                fs_pair_sel_cb pair_sel, void *user);
+/* The same search over the subtrees of `count` given open nodes (perms
+ * count x n, cursors and bounds; node 0 at the bottom of the stack, the
+ * last one taken first) instead of the root: the sequential counterpart of
+ * seeding a GPU search with open nodes. */
+int fs_explore_seeded(const fs_bound *b, const int32_t *perms, const int32_t *l1,
+                      const int32_t *l2, const int32_t *lbs, int64_t count, int32_t ub0,
+                      int32_t best, int64_t node_cap, fs_stats *stats, int32_t *best_perm);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(HERE, "_build", "liboracle.so")
 _REF_LIB = os.path.join(HERE, "_ref", "libref_bound.so")
 _REF_EXPLORE = os.path.join(HERE, "_ref", "ref_explore")
+# the reference's search built with MAX_NBJOBS = 64 (oracle/build.sh)
+_REF_EXPLORE_BIG = os.path.join(HERE, "_ref", "ref_explore_big")
 
 INT32_MAX = 2**31 - 1
 
@@ -56,6 +58,9 @@ def lib():
         L.fs_makespan.argtypes = [C.c_void_p, _i32p]
         L.fs_bound_eval_batch.argtypes = [C.c_void_p, _i32p, _i32p, _i32p, C.c_int64,
                                           _i32p, C.c_void_p, C.c_int]
+        L.fs_explore_seeded.argtypes = [C.c_void_p, _i32p, _i32p, _i32p, _i32p, C.c_int64,
+                                        C.c_int32, C.c_int32, C.c_int64, C.c_void_p,
+                                        C.c_void_p]
         L.fs_lb1_eval_batch.argtypes = [C.c_void_p, _i32p, _i32p, _i32p, C.c_int64, _i32p]
         L.fs_random_pool.argtypes = [C.c_uint64, C.c_int, C.c_int64, C.c_double,
                                      _i32p, _i32p, _i32p]
@@ -72,13 +77,17 @@ class FsStats(C.Structure):
     _fields_ = [("branched", C.c_int64), ("pruned", C.c_int64), ("leaves", C.c_int64),
                 ("improved", C.c_int64), ("bounded", C.c_int64),
                 ("early_exits", C.c_int64), ("best_cost", C.c_int32), ("pad", C.c_int32),
-                ("coverage_lo", C.c_uint64), ("coverage_hi", C.c_uint64)]
+                ("depth_hist", C.c_uint64 * 129)]
 
-    def as_dict(self) -> dict:
+    def as_dict(self, n: int) -> dict:
+        """Counters; coverage = sum over pruned nodes and leaves of
+        (n - depth)! (src/weights.cpp:11-22), in exact integers."""
+        import math
         return {"branched": self.branched, "pruned": self.pruned, "leaves": self.leaves,
                 "improved": self.improved, "bounded": self.bounded,
                 "early_exits": self.early_exits, "best_cost": self.best_cost,
-                "coverage": (self.coverage_hi << 64) | self.coverage_lo}
+                "coverage": sum(int(self.depth_hist[d]) * math.factorial(n - d)
+                                for d in range(n + 1))}
 
 
 LOG_CB = C.CFUNCTYPE(None, C.POINTER(C.c_int32), C.c_int, C.c_int, C.c_int32, C.c_int32,
@@ -186,13 +195,32 @@ class Bound:
                               int(node_cap), C.byref(st), perm.ctypes.data,
                               C.cast(lcb, C.c_void_p) if lcb else None,
                               C.cast(scb, C.c_void_p) if scb else None, None)
-        return rc, st.as_dict(), perm
+        return rc, st.as_dict(self.n), perm
+
+    def explore_seeded(self, perms, l1, l2, lbs, ub0: int | None = None, best: int = 99999,
+                       node_cap: int = 0):
+        """The sequential DFS over the subtrees of given open nodes (row 0 at
+        the stack bottom, the last row taken first); returns (rc, stats, perm)."""
+        perms = np.ascontiguousarray(perms, dtype=np.int32).reshape(-1, self.n)
+        l1 = np.ascontiguousarray(l1, dtype=np.int32)
+        l2 = np.ascontiguousarray(l2, dtype=np.int32)
+        lbs = np.ascontiguousarray(lbs, dtype=np.int32)
+        st = FsStats()
+        perm = np.full(self.n, -1, dtype=np.int32)
+        rc = lib().fs_explore_seeded(self.h, perms, l1, l2, lbs, len(l1),
+                                     INT32_MAX if ub0 is None else int(ub0), int(best),
+                                     int(node_cap), C.byref(st), perm.ctypes.data)
+        return rc, st.as_dict(self.n), perm
 
 
 # ---------------------------------------------------------------- reference
 
 def have_reference() -> bool:
     return os.path.exists(_REF_LIB) and os.path.exists(_REF_EXPLORE)
+
+
+def have_reference_big() -> bool:
+    return have_reference() and os.path.exists(_REF_EXPLORE_BIG)
 
 
 _ref = None
@@ -253,11 +281,16 @@ def ref_explore(p: np.ndarray, ub0: int | None = None, best: int = 99999,
     """Run the reference's CPU search (oracle/_ref/ref_explore) on `p`.
     `workdir`: the working directory, where the reference reads its initial
     incumbents from bab.solutions (with ub0 None, a file already there is
-    kept) and appends every improvement to it; a temporary one if None."""
+    kept) and appends every improvement to it; a temporary one if None.
+    Instances with n > 20 run on the reference's sources rebuilt with
+    MAX_NBJOBS = 64 (oracle/_ref/ref_explore_big)."""
     m, n = p.shape
+    exe = _REF_EXPLORE if n <= 20 else _REF_EXPLORE_BIG
+    if n > 64:
+        raise ValueError("the reference's search is built for n <= 64")
     with tempfile.TemporaryDirectory() as tmp:
         d = workdir or tmp
-        r = subprocess.run([_REF_EXPLORE, str(n), str(m), str(-1 if ub0 is None else ub0),
+        r = subprocess.run([exe, str(n), str(m), str(-1 if ub0 is None else ub0),
                             str(best), d.rstrip("/") + "/"],
                            input=" ".join(str(int(x)) for x in p.ravel()),
                            capture_output=True, text=True, timeout=timeout, check=True)

@@ -1,6 +1,6 @@
 // TEST INFRASTRUCTURE (oracle pin only). Shared set-up for the harnesses
 // that drive the reference's own compiled translation units (built in place
-// from the reference's src/ by oracle/build_ref.sh; nothing from the
+// from the reference's src/ by oracle/build.sh; nothing from the
 // reference is copied into this repository).
 //
 // What the reference's src/pbab.cpp:30-80 and src/arguments.cpp:6-35 would

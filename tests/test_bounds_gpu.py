@@ -1,7 +1,8 @@
 """GPU parity of the pool bound kernels, through the C-ABI.
 
 Bit-exact against (1) the reference's own outputs in tests/golden and
-(2) the CPU oracle on seeded pools of n=20, m=20, seeds 0-9; at 2^20
+(2) the CPU oracle on seeded pools of n=20, m=20, seeds 0-9, every pool size
+from 2^16 to 2^20 records, and on frontiers logged from the search; at 2^20
 records, size-independent properties (leaf bounds equal makespans, LB2 never
 exceeds the makespan of the record's own completion, repeat launches agree).
 """
@@ -53,13 +54,44 @@ def test_lb2_matches_reference_golden(torch_cuda, W, golden_pools):
 
 @pytest.mark.parametrize("seed", range(10))
 def test_lb2_matches_oracle_n20_m20(torch_cuda, W, oracle, seed):
-    n, m, count = 20, 20, 1 << 14
+    """The pool-bound workload at its own sizes: for each seed, uniform
+    random pools of 2^16, 2^17, ..., 2^20 records, every bound bit-exact
+    against the oracle."""
+    import os
+    n, m = 20, 20
     p = W.gen_instance(seed, n, m)
-    recs = W.gen_pool(1000 + seed, n, count, leaf_share=0.02)
-    got = run_dev(torch_cuda, W.Context(p), recs)
+    ctx = W.Context(p)
+    ob = oracle.Bound(p)
+    for k, log2 in enumerate(range(16, 21)):
+        recs = W.gen_pool(1000 + 8 * seed + k, n, 1 << log2, leaf_share=0.02)
+        got = run_dev(torch_cuda, ctx, recs)
+        perms, l1, l2 = W.unpack_records(recs, n)
+        want = ob.eval_batch(perms, l1, l2, nthreads=os.cpu_count() or 8)
+        np.testing.assert_array_equal(got, want, err_msg=f"seed {seed} pool 2^{log2}")
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_lb2_matches_oracle_on_search_frontiers(torch_cuda, W, oracle, seed):
+    """Pools of the kind the search bounds: 2^16 children logged from the
+    exact search on each instance (uneven depths, both sides), bounded by
+    the pool kernel and the oracle."""
+    import os
+    import torch
+    from wsbb_gb300 import learned
+    n, m, count = 20, 20, 1 << 16
+    p = W.gen_instance(seed, n, m)
+    ctx = W.Context(p)
+    neh, _ = W.neh(p)
+    buf = torch.zeros((count, W.node_stride(n) // 2), dtype=torch.int16, device="cuda")
+    got_n, _ = learned.log_nodes(ctx, buf.data_ptr(), count, 3, ub0=neh, window=1024)
+    torch.cuda.synchronize()
+    assert got_n > count // 2
+    recs = buf[:got_n].cpu().numpy()
     perms, l1, l2 = W.unpack_records(recs, n)
-    want = oracle.Bound(p).eval_batch(perms, l1, l2, nthreads=8)
-    np.testing.assert_array_equal(got, want)
+    assert len(np.unique(l2 - l1)) > 5  # many depths
+    np.testing.assert_array_equal(
+        run_dev(torch_cuda, ctx, recs),
+        oracle.Bound(p).eval_batch(perms, l1, l2, nthreads=os.cpu_count() or 8))
 
 
 @pytest.mark.parametrize("n,m,seed", [(20, 5, 0), (20, 10, 1), (50, 10, 2), (50, 20, 3),

@@ -16,12 +16,25 @@ import tempfile
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("WSBB_REFERENCE_DIR", "/root/reference")
+
+
+def reference_dir():
+    """WSBB_REFERENCE_DIR, else the tree oracle/build.sh compiled the
+    reference from (recorded in oracle/_ref/reference_dir); None if neither."""
+    ref = os.environ.get("WSBB_REFERENCE_DIR")
+    if not ref:
+        rec = os.path.join(ROOT, "oracle", "_ref", "reference_dir")
+        if os.path.exists(rec):
+            with open(rec) as f:
+                ref = f.read().strip()
+    return ref if ref and os.path.isdir(os.path.join(ref, "headers")) else None
 
 
 def test_documented_bound_plugin_compiles_against_the_reference_interface():
-    if not os.path.isdir(os.path.join(REF, "headers")) or shutil.which("g++") is None:
-        pytest.skip("reference tree or g++ not available")
+    REF = reference_dir()
+    if REF is None or shutil.which("g++") is None:
+        pytest.skip("reference tree not given (WSBB_REFERENCE_DIR) nor built by "
+                    "oracle/build.sh, or g++ not available")
     with open(os.path.join(ROOT, "INTEGRATION.md")) as f:
         blocks = re.findall(r"```cpp\n(.*?)```", f.read(), flags=re.S)
     plugin = blocks[0]

@@ -52,6 +52,29 @@ def test_oracle_search_matches_reference(oracle, golden_explore):
             assert list(perm) == run["perm"], tag
 
 
+def test_oracle_search_matches_reference_above_n20(oracle):
+    """The reference's own search rebuilt for n <= 64 (explore_big.json):
+    n = 30 to 50, up to 530k child bounds per run — every counter, the
+    optimum, its permutation and coverage = n!."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "explore_big.json")) as f:
+        runs = json.load(f)["runs"]
+    assert max(r["n"] for r in runs) == 50 and len(runs) >= 20
+    for run in runs:
+        p = oracle.gen_instance(run["seed"], run["n"], run["m"])
+        assert oracle.neh(p)[0] == run["neh"]
+        rc, st, perm = oracle.Bound(p).explore(ub0=run["ub0"], best=run["best"])
+        tag = f"n{run['n']} m{run['m']} s{run['seed']} best={run['best']}"
+        assert rc == 0, tag
+        for k in ("branched", "pruned", "leaves", "improved", "bounded"):
+            assert st[k] == run[k], f"{tag}: {k}"
+        assert st["best_cost"] == run["optimum"], tag
+        assert str(st["coverage"]) == run["coverage"] == str(math.factorial(run["n"])), tag
+        if run["perm"] is not None:
+            assert list(perm) == run["perm"], tag
+
+
 def test_coverage_is_n_factorial(oracle, golden_explore):
     import math
     for run in golden_explore:
@@ -139,3 +162,22 @@ def test_oracle_matches_the_reference_on_a_sweep(oracle):
         perms, l1, l2 = oracle.random_pool(s, n, 400, 0.1)
         np.testing.assert_array_equal(oracle.Bound(p).eval_batch(perms, l1, l2),
                                       oracle.RefBound(p).eval_batch(perms, l1, l2))
+
+
+@pytest.mark.skipif("not __import__('oracle.oracle', fromlist=['x']).have_reference_big()")
+def test_oracle_matches_the_reference_above_n20_live(oracle):
+    """Where the reference is built: its search compiled for n <= 64, run
+    live at n = 25 to 50 next to the oracle."""
+    for s, n, m in [(5, 45, 7), (8, 50, 5), (9, 50, 10), (2, 26, 4)]:
+        p = oracle.gen_instance(s, n, m)
+        ub, _ = oracle.neh(p)
+        for best in (99999, ub):
+            r = oracle.ref_explore(p, ub0=ub, best=best)
+            rc, st, perm = oracle.Bound(p).explore(ub0=ub, best=best, node_cap=2_000_000)
+            assert rc == 0
+            for k in ("branched", "pruned", "leaves", "improved", "bounded"):
+                assert st[k] == r[k], (s, n, m, best, k)
+            assert st["best_cost"] == r["optimum"]
+            assert st["coverage"] == int(r["coverage"]) == math.factorial(n)
+            if st["improved"]:
+                assert list(perm) == list(r["perm"])

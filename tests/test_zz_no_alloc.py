@@ -77,3 +77,47 @@ def test_noalloc_rejects_what_does_not_fit(mods):
     rc, got = run(L, "wsbb_explore_noalloc", ctx, E, INT32_MAX, 99999, window=64)
     assert rc == 0 and got.status == 0
     np.testing.assert_equal(got.best_cost > 0, True)
+
+
+def test_noalloc_overflow_then_recovers(mods):
+    """A stack just above one rewrite region overflows part-way through a
+    search without an incumbent: the call returns WSBB_ERR_CAPACITY, and
+    the next call with the derived defaults runs the whole search and
+    equals the allocating search."""
+    W, E, L = mods
+    n = 20
+    p = W.gen_instance(2, n, 5)
+    ctx = W.Context(p)
+    region = 4 * 64 + 4096  # the no-alloc region reserve at window 64
+    rc, _ = run(L, "wsbb_explore_noalloc", ctx, E, INT32_MAX, 99999, window=64,
+                capacity=region + 256)
+    assert rc == -6, L.wsbb_last_error(ctx.h)
+    ub, _ = W.neh(p)
+    rc, want = run(L, "wsbb_explore", ctx, E, ub, 99999, window=256)
+    assert rc == 0
+    rc, got = run(L, "wsbb_explore_noalloc", ctx, E, ub, 99999)
+    assert rc == 0 and got.status == 0, L.wsbb_last_error(ctx.h)
+    for k in KEYS:
+        assert getattr(got, k) == getattr(want, k), k
+    assert list(got.depth_hist) == list(want.depth_hist)
+
+
+def test_noalloc_call_leaves_free_memory_unchanged(mods):
+    """Free device memory is the same before and after a call (the first
+    call of the module, which may load the library's device code, is made
+    before the measurement)."""
+    import torch
+    W, E, L = mods
+    p = W.gen_instance(4, 16, 8)
+    ctx = W.Context(p)
+    ub, _ = W.neh(p)
+    rc, _ = run(L, "wsbb_explore_noalloc", ctx, E, ub, 99999)
+    assert rc == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        rc, st = run(L, "wsbb_explore_noalloc", ctx, E, ub, 99999)
+        assert rc == 0 and st.status == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0

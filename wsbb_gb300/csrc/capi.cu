@@ -93,6 +93,8 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 		e = cudaMalloc(&ctx->d_claim, sizeof(unsigned long long));
 	if (e == cudaSuccess)
 		e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess)
+		e = cudaEventCreateWithFlags(&ctx->legacy_ev, cudaEventDisableTiming);
 	if (e != cudaSuccess) {
 		fprintf(stderr, "wsbb_ctx_create: %s\n", cudaGetErrorString(e));
 		wsbb_ctx_destroy(ctx);
@@ -141,6 +143,8 @@ extern "C" void wsbb_ctx_destroy(wsbb_ctx *ctx)
 		cudaFree(ctx->d_claim);
 	if (ctx->stream)
 		cudaStreamDestroy(ctx->stream);
+	if (ctx->legacy_ev)
+		cudaEventDestroy(ctx->legacy_ev);
 	delete ctx;
 }
 

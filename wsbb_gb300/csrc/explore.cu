@@ -61,7 +61,6 @@
 #include <chrono>
 #include <climits>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "node_features.cuh"
@@ -115,6 +114,13 @@ struct ExDev {
 	long long exported;            // nodes the last export took
 	unsigned long long log_count;  // training records written
 	unsigned long long hist[WSBB_MAX_JOBS + 1];
+	// pend[d]: children of the open ancestor at depth d (of the next node
+	// the sequential search takes) that were pruned at birth. They are
+	// counted when their father commits, but the sequential search takes
+	// them only after the father's open children's subtrees, when the
+	// father's block closes; a stopped search subtracts them to report the
+	// exact sequential prefix.
+	unsigned pend[WSBB_MAX_JOBS + 1];
 };
 
 struct ExParams {
@@ -218,6 +224,41 @@ __device__ T block_reduce(T v, Op op, T identity, T *scratch)
 	return total;
 }
 
+// Block-wide exclusive suffix scan for NT threads: thread t receives
+// op over the values of threads t + 1 .. NT - 1 (identity for the last).
+template <int NT, typename T, typename Op>
+__device__ T block_excl_suffix_scan(T v, Op op, T identity, T *scratch)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	constexpr int NW = NT / 32;
+	T x = v;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		T y = __shfl_down_sync(0xffffffffu, x, d);
+		if (lane + d < 32)
+			x = op(x, y);
+	}
+	if (lane == 0)
+		scratch[warp] = x; // inclusive suffix of the warp
+	__syncthreads();
+	if (warp == 0) {
+		T w = lane < NW ? scratch[lane] : identity;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			T y = __shfl_down_sync(0xffffffffu, w, d);
+			if (lane + d < 32)
+				w = op(w, y);
+		}
+		scratch[lane] = w; // inclusive suffix over warps
+	}
+	__syncthreads();
+	const T warp_suffix = warp == NW - 1 ? identity : scratch[warp + 1];
+	const T excl_in_warp = __shfl_down_sync(0xffffffffu, x, 1);
+	const T excl = lane == 31 ? warp_suffix : op(warp_suffix, excl_in_warp);
+	__syncthreads();
+	return excl;
+}
+
 struct MinOp {
 	__device__ int operator()(int a, int b) const { return a < b ? a : b; }
 };
@@ -285,6 +326,10 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 	__shared__ unsigned long long s_cnt[6];
 	// per-iteration depth counts (at most window * n each: 32 bits)
 	__shared__ unsigned s_hist[WSBB_MAX_JOBS + 1];
+	// pending pruned-at-birth children per depth of their father (ExDev::pend)
+	// and, within a round, the npruned of the round's suffix-minimum markers
+	__shared__ unsigned s_pend[WSBB_MAX_JOBS + 1], s_sfx[WSBB_MAX_JOBS + 1];
+	__shared__ int s_dmin;
 	ExDev *D = P.dev;
 	if (halted(D))
 		return;
@@ -292,8 +337,11 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 	const int n = P.n;
 	if (t < 6)
 		s_cnt[t] = 0;
-	for (int i = t; i <= n; i += kSelThreads)
+	for (int i = t; i <= n; i += kSelThreads) {
 		s_hist[i] = 0;
+		s_pend[i] = D->pend[i];
+		s_sfx[i] = 0;
+	}
 	__syncthreads();
 
 	long long top = D->top;
@@ -392,6 +440,53 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 				P.best_rec[b] = P.rec[src * P.stride + b];
 			ub = cmin;
 		}
+		// Open blocks. A committed entry of depth e closes the block of every
+		// father of depth >= e (the sequential search has taken that
+		// father's pruned-at-birth children just before it); a committed
+		// marker opens its own. After the round, pend[d] for d >= the
+		// round's smallest depth belongs to the last entry of depth <= d:
+		// its npruned if it has depth d and is a marker, else 0. Those last
+		// entries are the round's suffix minima of depth (distinct depths).
+		{
+			int loc_min = INT_MAX;
+			bool has_np = false;
+#pragma unroll
+			for (int i = 0; i < kItems; ++i) {
+				const int g = kItems * t + i;
+				const bool pop = g < s && e[i].state != ST_DEAD && e[i].state != ST_EXPORTED;
+				if (pop) {
+					loc_min = min(loc_min, int(e[i].depth));
+					has_np |= e[i].state == ST_BRANCHED && e[i].npruned;
+				}
+			}
+			if (__syncthreads_or(has_np)) {
+				int later = block_excl_suffix_scan<kSelThreads>(loc_min, MinOp(), INT_MAX, s_int);
+				if (t == 0)
+					s_dmin = min(later, loc_min);
+#pragma unroll
+				for (int i = kItems - 1; i >= 0; --i) {
+					const int g = kItems * t + i;
+					const bool pop = g < s && e[i].state != ST_DEAD && e[i].state != ST_EXPORTED;
+					if (pop && int(e[i].depth) < later) {
+						if (e[i].state == ST_BRANCHED)
+							s_sfx[e[i].depth] = e[i].npruned;
+						later = e[i].depth;
+					}
+				}
+				__syncthreads();
+			} else {
+				const int dm = block_reduce<kSelThreads>(loc_min, MinOp(), INT_MAX, s_int);
+				if (t == 0)
+					s_dmin = dm;
+				__syncthreads();
+			}
+			const int dmin = s_dmin;
+			for (int d = t; d <= n; d += kSelThreads) {
+				if (d >= dmin)
+					s_pend[d] = s_sfx[d];
+				s_sfx[d] = 0;
+			}
+		}
 		top -= s;
 		if (t == 0)
 			D->committed += (unsigned long long)s;
@@ -409,6 +504,9 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 			c_pr++;
 			atomicAdd(&s_hist[stopper.depth], 1u);
 		}
+		for (int d = t; d <= n; d += kSelThreads)
+			if (d >= stopper.depth)
+				s_pend[d] = 0; // the pruned marker closes deeper blocks
 		top -= 1;
 		while (top >= 0) {
 			int out_at = kChunk;
@@ -468,9 +566,12 @@ __global__ void __launch_bounds__(kSelThreads) commit_kernel(ExParams P)
 		if (top < 0)
 			D->done = 1;
 	}
-	for (int i = t; i <= n; i += kSelThreads)
+	for (int i = t; i <= n; i += kSelThreads) {
 		if (s_hist[i])
 			D->hist[i] += s_hist[i];
+		// the stack bottom closes every block
+		D->pend[i] = top < 0 ? 0u : s_pend[i];
+	}
 }
 
 // ---- doom: stop expanding under markers the new incumbent condemns ----------
@@ -1495,6 +1596,13 @@ void fill_stats(const wsbb::ExDev &h, const int16_t *best_rec, int n, int status
 	st->early = (int64_t)h.early;
 	st->settled_fathers = (int64_t)h.settled_fathers;
 	st->d2h_bytes = (int64_t)(reads * (long long)sizeof(wsbb::ExDev) + S);
+	long long pending = 0;
+	for (int d = 0; d < n; ++d) {
+		st->pending_hist[d + 1] = h.pend[d];
+		pending += h.pend[d];
+	}
+	st->pending = pending;
+	st->takes = st->branched + st->pruned + st->leaves - pending;
 }
 
 struct SearchMode {
@@ -1615,7 +1723,7 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
 	// no caller stream: the training-record buffer may still be in use by
 	// work queued on the legacy default stream
-	if (!stream_v && (e = wait_for_legacy(s)) != cudaSuccess)
+	if (!stream_v && (e = wait_for_legacy(s, ctx->legacy_ev)) != cudaSuccess)
 		return ex_fail(ctx, e, "stream ordering");
 	if (resume)
 		resume_kernel<<<1, 32, 0, s>>>(X->P, cfg->ub0, cfg->best);
@@ -1868,27 +1976,47 @@ namespace {
 
 __device__ __align__(256) uint8_t g_noalloc_scratch[WSBB_NOALLOC_SCRATCH_BYTES];
 
-// Device address of g_noalloc_scratch, looked up once per device. In host
-// code the symbol itself is only a host-side stand-in, never a device
-// address, so it is never handed to a kernel directly.
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[64];
-
+// Device address of g_noalloc_scratch on the current device. In host code
+// the symbol itself is only a host-side stand-in, never a device address,
+// so it is never handed to a kernel directly. The address is looked up on
+// every call (a cheap query once the module is loaded), so a primary
+// context that was torn down and re-created never leaves a stale pointer.
 int noalloc_scratch(wsbb_ctx *ctx, uint8_t **out)
 {
-	if (ctx->device < 0 || ctx->device >= 64)
-		return wsbb_set_error(ctx, WSBB_ERR_ARG, "device ordinal out of range");
-	std::lock_guard<std::mutex> lock(g_noalloc_mu);
-	if (!g_noalloc_addr[ctx->device]) {
-		void *p = nullptr;
-		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-		if (e != cudaSuccess || !p)
-			return ex_fail(ctx, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
-			               "cudaGetSymbolAddress(no-alloc scratch)");
-		g_noalloc_addr[ctx->device] = p;
-	}
-	*out = static_cast<uint8_t *>(g_noalloc_addr[ctx->device]);
+	void *p = nullptr;
+	const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+	if (e != cudaSuccess || !p)
+		return ex_fail(ctx, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+		               "cudaGetSymbolAddress(no-alloc scratch)");
+	*out = static_cast<uint8_t *>(p);
 	return WSBB_OK;
+}
+
+// Stack capacity (nodes) that fits the fixed array with the given window
+// and the region reserve of the no-alloc search (0: none).
+long long noalloc_capacity(int window, long long region_cap, int n, int S)
+{
+	const size_t limit = WSBB_NOALLOC_SCRATCH_BYTES;
+	wsbb::ExParams P{};
+	const size_t fixed = wsbb::search_layout(nullptr, 0, region_cap, window, n, S, P);
+	long long cap = fixed < limit ? (long long)((limit - fixed) / (S + sizeof(wsbb::Meta))) : 0;
+	while (cap > 0 && wsbb::search_layout(nullptr, cap, region_cap, window, n, S, P) > limit)
+		cap -= 256;
+	return std::max(cap, 0ll);
+}
+
+long long noalloc_region(int window) { return 4ll * window + 4096; }
+
+// Default window: the widest of 1024, 512, ..., 64 that leaves the stack
+// room for at least 8 iterations of `window` fathers with n children each
+// (n = 20: 1024 and ~397k nodes; n = 50: 256 and ~178k; n = 100: 64 and
+// ~99k).
+int noalloc_default_window(int n, int S)
+{
+	for (int w = 1024; w > 64; w >>= 1)
+		if (noalloc_capacity(w, noalloc_region(w), n, S) >= 8ll * w * n)
+			return w;
+	return 64;
 }
 
 }  // namespace
@@ -1912,19 +2040,15 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 
 	const int n = ctx->inst.n;
 	const int S = ctx->bp.stride;
-	const int window = cfg->window > 0 ? cfg->window : 1024;
+	const int window = cfg->window > 0 ? cfg->window : noalloc_default_window(n, S);
 	const size_t limit = WSBB_NOALLOC_SCRATCH_BYTES;
 	ExploreState X; // host-side view only: no graph, no allocation
 	if (window > (1 << 20))
 		return wsbb_set_error(ctx, WSBB_ERR_ARG, "window out of range");
-	const long long region_cap = 4ll * window + 4096;
+	const long long region_cap = noalloc_region(window);
 	long long cap = cfg->capacity;
-	if (cap <= 0) {
-		const size_t fixed = search_layout(nullptr, 0, region_cap, window, n, S, X.P);
-		cap = fixed < limit ? (long long)((limit - fixed) / (S + sizeof(Meta))) : 0;
-		while (cap > 0 && search_layout(nullptr, cap, region_cap, window, n, S, X.P) > limit)
-			cap -= 256;
-	}
+	if (cap <= 0)
+		cap = noalloc_capacity(window, region_cap, n, S);
 	if (cap < region_cap || search_layout(nullptr, cap, region_cap, window, n, S, X.P) > limit)
 		return wsbb_set_error(ctx, WSBB_ERR_CAPACITY,
 		                      "window / capacity do not fit the fixed no-alloc scratch of " +
@@ -1940,6 +2064,11 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	X.fam_kb = cfg->family_smem_kb;
 
 	cudaStream_t s = stream_v ? static_cast<cudaStream_t>(stream_v) : ctx->stream;
+	// no caller stream: the search runs on the context's stream after the
+	// work queued on the legacy default stream so far (the context's own
+	// event, so nothing is created here)
+	if (!stream_v && (e = wait_for_legacy(s, ctx->legacy_ev)) != cudaSuccess)
+		return ex_fail(ctx, e, "stream ordering");
 	const auto t0 = std::chrono::steady_clock::now();
 	init_kernel<<<1, 128, 0, s>>>(X.P, cfg->ub0, cfg->best, window_min_of(window), window);
 	e = cudaGetLastError();

@@ -141,10 +141,16 @@ cudaError_t allow_max_dynamic_smem(K kernel)
 // legacy default stream, where a caller given no stream (PyTorch's default
 // stream among them) writes the buffers it passes in. A non-blocking
 // stream does not wait on the legacy stream by itself.
-inline cudaError_t wait_for_legacy(cudaStream_t s)
+// `s` waits for the work queued on the legacy default stream so far, with
+// an event of the caller's (`ev`), or one made for the call when ev is null.
+inline cudaError_t wait_for_legacy(cudaStream_t s, cudaEvent_t ev_given = nullptr)
 {
 	if (s == nullptr || s == cudaStreamLegacy)
 		return cudaSuccess;
+	if (ev_given) {
+		const cudaError_t e = cudaEventRecord(ev_given, cudaStreamLegacy);
+		return e == cudaSuccess ? cudaStreamWaitEvent(s, ev_given, 0) : e;
+	}
 	cudaEvent_t ev;
 	cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
 	if (e != cudaSuccess)
@@ -171,6 +177,9 @@ struct wsbb_ctx {
 	int64_t host_cap = 0;
 	unsigned long long *d_claim = nullptr; // family bounds' father counter
 	cudaStream_t stream = nullptr;
+	// recorded on the legacy default stream when a call given no stream runs
+	// on `stream` (created with the context, so such calls make no event)
+	cudaEvent_t legacy_ev = nullptr;
 	// search state (explore.cu)
 	struct ExploreState *ex = nullptr;
 };

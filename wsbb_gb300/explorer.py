@@ -33,7 +33,9 @@ class ExploreStats(C.Structure):
                 ("status", C.c_int32), ("depth_hist", C.c_uint64 * (MAX_JOBS + 1)),
                 ("best_perm", C.c_int32 * MAX_JOBS), ("seconds", C.c_double),
                 ("scanned", C.c_int64), ("committed", C.c_int64), ("early", C.c_int64),
-                ("settled_fathers", C.c_int64), ("d2h_bytes", C.c_int64)]
+                ("settled_fathers", C.c_int64), ("d2h_bytes", C.c_int64),
+                ("takes", C.c_int64), ("pending", C.c_int64),
+                ("pending_hist", C.c_uint32 * (MAX_JOBS + 1))]
 
 
 NO_GRAPH = 1
@@ -120,4 +122,17 @@ def stats_dict(st: ExploreStats, n: int) -> dict:
             "coverage": coverage(st.depth_hist, n),
             "best_perm": np.array(st.best_perm[:n], dtype=np.int32),
             "seconds": st.seconds, "scanned": st.scanned, "committed": st.committed,
-            "d2h_bytes": st.d2h_bytes}
+            "d2h_bytes": st.d2h_bytes, "takes": st.takes, "pending": st.pending,
+            "depth_hist": [int(v) for v in st.depth_hist[:n + 1]],
+            "pending_hist": [int(v) for v in st.pending_hist[:n + 1]]}
+
+
+def sequential_prefix(stats: dict, n: int) -> dict:
+    """The sequential search's counters after exactly stats["takes"] takes
+    (the point where a stopped GPU search stands): children pruned at birth
+    whose take is still ahead are removed from pruned and the coverage."""
+    hist = [h - p for h, p in zip(stats["depth_hist"], stats["pending_hist"])]
+    return {"takes": stats["takes"], "branched": stats["branched"],
+            "pruned": stats["pruned"] - stats["pending"], "leaves": stats["leaves"],
+            "improved": stats["improved"], "bounded": stats["bounded"],
+            "best_cost": stats["best_cost"], "coverage": coverage(hist, n)}
