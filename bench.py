@@ -457,6 +457,17 @@ def run_gpu(args) -> None:
         sections = {"lb2_pool": lb2_pool_section(dev, stream, sptr, peak, 40)}
         if not args.no_proof:
             sections["time_to_proof"] = proof_section()
+        if args.proof_seconds > 0:
+            from wsbb_gb300 import proof_progress
+            sections["headline_proof_progress"] = {
+                "workload": f"the headline search (n={S_N} m={S_M} seed {seed}, NEH "
+                            f"incumbent) run for {args.proof_seconds:g} s of device time: "
+                            "the share of the n! permutations its exact prefix covers "
+                            "(the reference's coverage weights) and the time to proof "
+                            "extrapolated linearly from it",
+                "runs": [proof_progress.run(S_N, S_M, seed, mode, args.proof_seconds, window=win,
+                                            device=local)
+                         for mode in ("ub0", "default")]}
         if not args.no_multi:
             from wsbb_gb300 import multi_bench
             sections["multi_instance"] = multi_bench.run()
@@ -503,6 +514,9 @@ def main():
                     help="skip the time-to-proof section (n=50 m=10, seeds 0-4)")
     ap.add_argument("--no-multi", action="store_true",
                     help="skip the multi-instance section (64 concurrent instances)")
+    ap.add_argument("--proof-seconds", type=float, default=20.0,
+                    help="device seconds of the headline search per best setting for the "
+                         "proof-progress section (0: skip it)")
     ap.add_argument("--only", choices=["roofline"], default=None,
                     help="run one measurement alone (a small case for profilers)")
     args = ap.parse_args()

@@ -165,10 +165,13 @@ typedef struct {
 	                        16 window + 8192 */
 	int64_t max_iters;   /* stop after this many iterations (0: none) */
 	int32_t flags;       /* WSBB_EXPLORE_* */
-	int32_t family_smem_kb; /* shared memory per CTA of the family bounds (KB,
-	                           0: 56): the pair-chunk length, and with it how
-	                           many CTAs share an SM (a tile shape the
-	                           autotuner picks) */
+	int32_t family_smem_kb; /* form of the family bounds (a tile shape the
+	                           autotuner picks): 0 stages the instance's whole
+	                           packed Johnson table in shared memory when it
+	                           fits (times <= 127, m <= 20; else 56 applies);
+	                           > 0 bounds pairs in chunks whose rows take
+	                           this many KB of shared memory per CTA, which
+	                           also sets how many CTAs share an SM */
 	int64_t max_bounded; /* stop once this many tree nodes are bounded,
 	                        checked between graph launches (0: no limit);
 	                        the search commits in DFS order, so a budget is

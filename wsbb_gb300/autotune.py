@@ -3,9 +3,11 @@
 Two shapes set how the batched search maps onto the GPU:
   window          fathers branched per iteration (the batch: more work per
                   launch against more speculative work)
-  family_smem_kb  shared memory per CTA of the family bounds: how many
-                  machine pairs one chunk holds (their per-job X rows) and
-                  with it how many CTAs share an SM
+  family_smem_kb  the family bounds' form: 0 stages the whole packed
+                  Johnson table in shared memory (where the instance fits
+                  it, else it means 56); a budget in KB selects the chunked
+                  form, whose pair chunks hold their per-job X rows in that
+                  much shared memory, and with it how many CTAs share an SM
 Neither changes the tree. `tune` times the same prefix of the search for
 every candidate pair — the first `node_budget` tree nodes (the search
 commits in DFS order, so a node budget is the same tree prefix whatever the
@@ -24,7 +26,7 @@ import os
 import sys
 
 WINDOWS = (512, 1024, 2048, 4096, 8192, 16384, 32768)
-SMEM_KB = (56, 100, 160)
+SMEM_KB = (0, 56, 100, 160)
 
 
 def cache_path() -> str:

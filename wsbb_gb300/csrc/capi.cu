@@ -72,6 +72,9 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 	ctx->device = device;
 	wsbb::DeviceTables &T = ctx->tables;
 	T.bytes = H.img8.size() + H.img16.size() + H.imgT.size() + H.imgPos.size();
+	const size_t off_pack = (T.bytes + 255) & ~size_t(255);
+	if (!H.imgPack.empty())
+		T.bytes = off_pack + H.imgPack.size();
 	cudaError_t e = cudaSetDevice(device);
 	if (e == cudaSuccess)
 		e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
@@ -89,6 +92,9 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 	if (e == cudaSuccess)
 		e = cudaMemcpy(base + H.img8.size() + H.img16.size() + H.imgT.size(), H.imgPos.data(),
 		               H.imgPos.size(), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess && !H.imgPack.empty())
+		e = cudaMemcpy(base + off_pack, H.imgPack.data(), H.imgPack.size(),
+		               cudaMemcpyHostToDevice);
 	if (e == cudaSuccess)
 		e = cudaMalloc(&ctx->d_claim, sizeof(unsigned long long));
 	if (e == cudaSuccess)
@@ -106,6 +112,10 @@ extern "C" int wsbb_ctx_create(const int32_t *p, int n, int m, int device, wsbb_
 	T.t16.blob = H.img16.empty() ? nullptr : base + H.img8.size();
 	T.johnsonT = reinterpret_cast<const uint2 *>(base + H.img8.size() + H.img16.size());
 	T.jobposT = base + H.img8.size() + H.img16.size() + H.imgT.size();
+	if (!H.imgPack.empty()) {
+		T.tpack = reinterpret_cast<const uint32_t *>(base + off_pack);
+		T.Pp = H.Pp;
+	}
 	wsbb::BoundParams &bp = ctx->bp;
 	bp.t8 = T.t8;
 	bp.t16 = T.t16;

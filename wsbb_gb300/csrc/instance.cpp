@@ -245,6 +245,30 @@ HostTables pack_tables(const Instance &I, std::string &err)
 	for (int i = 0; i < I.P; ++i)
 		for (int q = 0; q < n; ++q)
 			H.imgPos[size_t(I.johnson[size_t(i) * n + q]) * I.P + i] = uint8_t(q);
+	// packed 32-bit entries, position-major, rows of Pp words (P rounded up
+	// to 64): job | p1 << 7 | p2 << 14 | (p1 + lag + p2) << 21, when every
+	// field fits
+	{
+		bool fits = n <= 128;
+		for (int i = 0; fits && i < I.P; ++i)
+			for (int j = 0; fits && j < n; ++j) {
+				const int p1 = I.p[I.mach0[i] * n + j], p2 = I.p[I.mach1[i] * n + j];
+				fits = p1 <= 127 && p2 <= 127 && p1 + I.lag[size_t(i) * n + j] + p2 <= 2047;
+			}
+		if (fits) {
+			H.Pp = (I.P + 63) / 64 * 64;
+			H.imgPack.assign(size_t(n) * H.Pp * 4, 0);
+			uint32_t *pk = reinterpret_cast<uint32_t *>(H.imgPack.data());
+			for (int i = 0; i < I.P; ++i)
+				for (int q = 0; q < n; ++q) {
+					const int j = I.johnson[size_t(i) * n + q];
+					const uint32_t p1 = uint32_t(I.p[I.mach0[i] * n + j]);
+					const uint32_t p2 = uint32_t(I.p[I.mach1[i] * n + j]);
+					const uint32_t c = p1 + uint32_t(I.lag[size_t(i) * n + j]) + p2;
+					pk[size_t(q) * H.Pp + i] = uint32_t(j) | p1 << 7 | p2 << 14 | c << 21;
+				}
+		}
+	}
 	if (H.t8.bytes > 200 * 1024)
 		err = "bound tables exceed the shared-memory budget (n * m too large)";
 	return H;

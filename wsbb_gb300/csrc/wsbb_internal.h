@@ -55,11 +55,18 @@ struct DeviceTables {
 	const uint2 *johnsonT = nullptr;
 	// jobposT[j * P + i] = position of job j in pair i's Johnson order
 	const uint8_t *jobposT = nullptr;
+	// The same entries packed in 32 bits, position-major with rows of Pp
+	// (P rounded up to 64) words: tpack[q * Pp + i] = job | p1 << 7 |
+	// p2 << 14 | (p1 + lag + p2) << 21. Null when an instance's values do
+	// not fit (n > 128, a time > 127 or p1 + lag + p2 > 2047).
+	const uint32_t *tpack = nullptr;
+	int Pp = 0;
 };
 
 // Host images of the tables; offsets are relative to each image.
 struct HostTables {
-	std::vector<uint8_t> img8, img16, imgT, imgPos;
+	std::vector<uint8_t> img8, img16, imgT, imgPos, imgPack;
+	int Pp = 0;
 	TableView t8, t16;
 };
 HostTables pack_tables(const Instance &inst, std::string &err);
