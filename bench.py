@@ -473,7 +473,10 @@ def run_gpu(args) -> None:
             sections["multi_instance"] = multi_bench.run()
             sections["multi_instance"]["workload"] = (
                 "64 instances, n in {20,50,100} x m in {5,10,20}, seeds 0-63, NEH incumbent, "
-                "best=NEH, one context and stream each, 8 host threads, <= 64 iterations each")
+                "best=NEH, each to its proof or 10^9 bounded nodes, all in one resident launch "
+                "(resident_full); arms compared at 2*10^7 nodes each: the resident launch, "
+                "64 graph-launched searches on 8 host threads, and per-child LB2 with and "
+                "without the learned test on the m=20 instances with a trained selector")
         if world == 1:
             cores = os.cpu_count() or 1
             cpu = cpu_search_rate(0, cores, 8.0)

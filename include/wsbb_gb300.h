@@ -217,6 +217,37 @@ int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
                  void *stream);
 
 /*
+ * The search of one or many instances in one launch of resident CTAs
+ * (replaces the reference's host-driven pipeline, explorer::_explore_cpu_gpu
+ * with gpu::decompose_on_cpu / gpu::prune, src/explorer.cu:154-305,
+ * src/gpu.cu:180-408, and its peers' work stealing between processes,
+ * src/work_stealing/node.cpp:154-162, by stealing between CTAs).
+ *
+ * One cooperative launch: each instance gets a group of CTAs that runs its
+ * iterations (the same phases as wsbb_explore, met at group barriers); in
+ * the bound phase each CTA of a group owns a share of the fathers and
+ * steals from its group's other shares when its own is empty, and CTAs
+ * whose instance has finished steal fathers from the instances still
+ * running. Same counters and trees as wsbb_explore with the same cfg
+ * (window, capacity, best, ub0, max_iters, max_bounded apply per instance;
+ * no WSBB_EXPLORE_RESUME, no WSBB_EXPLORE_CHILD_LB2). Instances must be on
+ * one device, fit the staged family bounds (times <= 127, m <= 20) and
+ * number at most the resident CTAs (twice the SM count for n = 50, m = 20).
+ * Every wait between CTAs gives up after opts->wait_ms (0: 2000 ms): the
+ * launch then ends with WSBB_ERR_WATCHDOG and the contexts stay usable.
+ * opts->self_test = 1 makes the first wait also wait for a flag that
+ * nothing sets, so that the watchdog must run out (a test of that path).
+ * opts may be NULL. stats[k]: instance k; `seconds` is the launch's time.
+ */
+typedef struct {
+	int32_t wait_ms;
+	int32_t self_test;
+} wsbb_resident_opts;
+#define WSBB_EXPLORE_RESIDENT 8 /* wsbb_explore: run as the resident search */
+int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count, const wsbb_explore_cfg *cfgs,
+                          const wsbb_resident_opts *opts, wsbb_stats *stats, void *stream);
+
+/*
  * Work hand-off between searches (the reference's peers hand each other
  * node lists, BB_PROBLEM_PACKET, src/work_stealing/node.cpp:524-560 and
  * 1240-1283).

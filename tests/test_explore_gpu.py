@@ -114,17 +114,19 @@ def test_autotuned_shapes_keep_the_tree():
 
 def test_concurrent_searches_on_many_contexts():
     """Searches on several contexts from several host threads at once (their
-    graph captures overlap): every arm completes with the same trees."""
+    graph captures overlap), and the same instances in one resident launch:
+    every arm ends with the same trees."""
     import torch
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from wsbb_gb300 import multi_bench
-    out = multi_bench.run(instances=9, threads=3, max_iters=16, window=512,
-                          arms=("family", "per_child"))
-    for arm in ("family", "per_child"):
+    out = multi_bench.run(instances=9, threads=3, cmp_budget=2 * 10**6, window=512,
+                          arms=("resident", "family", "per_child"), full=False)
+    for arm in ("resident", "family", "per_child"):
         a = out["arms"][arm]
-        assert a["instances"] == 9 and a["same_tree"], arm
-    assert out["arms"]["family"]["bounded"] == out["arms"]["per_child"]["bounded"] > 0
+        assert a["instances"] == 9 and a["same_tree"] and a["finished"], arm
+    assert (out["arms"]["resident"]["bounded"] == out["arms"]["family"]["bounded"] ==
+            out["arms"]["per_child"]["bounded"] > 0)
 
 
 def test_node_budget_stops_the_search():

@@ -25,9 +25,15 @@ def sources() -> list[str]:
                   if f.endswith((".cu", ".cpp")))
 
 
+# per-file flags: the resident search's CTAs exchange global data within one
+# launch, so its global loads are cached in L2 only (no stale L1 copies
+# across SMs)
+FILE_FLAGS = {"resident.cu": ["-Xptxas", "-dlcm=cg"]}
+
+
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
-    cmd = ["nvcc", *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = ["nvcc", *NVCC_FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

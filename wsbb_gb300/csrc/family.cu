@@ -53,6 +53,7 @@
 // two-halves max per slot.
 #include <algorithm>
 
+#include "family_staged.cuh"
 #include "wsbb_internal.h"
 
 namespace wsbb {
@@ -693,528 +694,24 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 	}
 }
 
-// ---- staged form --------------------------------------------------------
-//
-// The same bounds, organised around shared memory (plain bounds of fathers
-// whose pairs fit the walkers, P <= 192, with times that pack into the
-// 32-bit Johnson entries of DeviceTables::tpack and 16-bit staircase paths):
-//
-//  * the packed Johnson table is staged once per CTA, position-major with
-//    rows of Pp (a multiple of 64) words, so a warp of walkers (consecutive
-//    pairs) reading entries at any positions hits 32 distinct banks;
-//  * the forward pass leaves, per walk rank k, the prefix C (16 bits) and
-//    the position q in rows [k][Pp] (lanes walk in step, so these accesses
-//    are conflict-free too) and the backward pass reads them back instead
-//    of walking the position masks a second time;
-//  * the backward pass leaves X_j per pair and free position (its column,
-//    not the job), and the children's bounds are formed afterwards by every
-//    thread of the CTA, lanes on consecutive columns of one pair: the
-//    fronts and backs they read (per machine and column) and the X_j are
-//    consecutive words, and both children's three terms are computed as
-//    16-bit halves of one word (add, then one three-way and one two-way
-//    unsigned 16-bit maximum).
-struct StagedLayout {
-	int Pp, xcs, xvs, frs;
-	size_t off_T, off_Xr, off_Xq, off_Xc, off_VW, off_PK, off_HT, off_pt, off_pairs, off_F,
-	    off_G, off_fr, off_fidx, off_misc, bytes;
-};
-
-StagedLayout staged_layout(int n, int m, int P, int Pp)
-{
-	StagedLayout L;
-	L.Pp = Pp;
-	L.xcs = n | 1;
-	L.xvs = n;
-	auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
-	size_t off = 0;
-	L.off_T = off;
-	off = a16(off + size_t(n) * Pp * 4);
-	L.off_Xr = off; // the cross-slice reduction reuses it after the backward pass
-	off = a16(off + std::max(size_t(n) * Pp * 2, size_t(kFamThreads) * 4));
-	L.off_Xq = off;
-	off = a16(off + size_t(n) * Pp);
-	L.off_Xc = off;
-	off = a16(off + size_t(P) * L.xcs * 2);
-	L.off_VW = off;
-	off = a16(off + size_t(m) * L.xvs * 8);
-	L.off_PK = off;
-	off = a16(off + size_t(P) * 16);
-	L.off_HT = off;
-	off = a16(off + 64 * 4);
-	L.off_pt = off;
-	off = a16(off + size_t(m) * (n + 1) * 2);
-	L.off_pairs = off;
-	off = a16(off + size_t(P) * 4);
-	L.off_F = off;
-	off = a16(off + 32 * 4);
-	L.off_G = off;
-	off = a16(off + 32 * 4);
-	L.frs = (n + 4 + 7) & ~7; // two record buffers
-	L.off_fr = off;
-	off = a16(off + size_t(2 * L.frs) * 2);
-	L.off_fidx = off;
-	off = a16(off + size_t(n));
-	L.off_misc = off; // two 4-word job masks, then two claimed fathers
-	off += 32 + 16;
-	L.bytes = a16(off);
-	return L;
-}
-
-// Free positions of a walk mask in ascending order (words w[0..NW-1]).
-template <int NW>
-__device__ __forceinline__ int pop_lowest(uint32_t (&w)[NW])
-{
-	int wi = NW - 1;
-#pragma unroll
-	for (int i = NW - 2; i >= 0; --i)
-		wi = w[i] ? i : wi;
-	uint32_t v = w[0];
-#pragma unroll
-	for (int i = 1; i < NW; ++i)
-		v = wi == i ? w[i] : v;
-	const int b = __ffs(v) - 1;
-#pragma unroll
-	for (int i = 0; i < NW; ++i)
-		if (wi == i)
-			w[i] = v & (v - 1);
-	return 32 * wi + b;
-}
-
-template <int NW>
-__device__ __forceinline__ bool mask_has(const uint32_t (&w)[NW], int job)
-{
-	uint32_t v = w[0];
-#pragma unroll
-	for (int i = 1; i < NW; ++i)
-		v = (job >> 5) == i ? w[i] : v;
-	return ((v >> (job & 31)) & 1u) != 0;
-}
-
-// Fronts and backs of the children by column (free position i): per
-// machine k four 16-bit values, vm = the time job j starts on k in the
-// BEGIN child's front, v = when it ends there, wm / w the same for the END
-// child's back. Warp 0 the father's front F and the fronts, warp 1 its
-// reversed back G and the backs (each a wavefront, lane = machine, then one
-// lane per free job).
-__device__ __forceinline__ void staged_fronts(int warp, int lane, int n, int m, int l1, int l2,
-                                              int u, int xvs, const uint16_t *pt,
-                                              const int16_t *fr, int32_t *F, int32_t *G,
-                                              uint16_t *VW16)
-{
-	const int ld = n + 1;
-	if (warp == 0) {
-		int32_t Fk = 0;
-		const int nj = l1 + 1;
-		int32_t add = (lane < m && lane == 0 && nj > 0) ? pt[fr[0]] : 0;
-		for (int s = 0; s < nj + m - 1; ++s) {
-			const int i = s - lane, i1 = i + 1;
-			const int32_t next = (lane < m && i1 >= 0 && i1 < nj) ? pt[lane * ld + fr[i1]] : 0;
-			const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
-			if (lane < m && i >= 0 && i < nj)
-				Fk = max(Fk, lane > 0 ? left : 0) + add;
-			add = next;
-		}
-		if (lane < m)
-			F[lane] = Fk;
-		__syncwarp();
-		for (int i = lane; i < u; i += 32) {
-			const int j = fr[l1 + 1 + i];
-			int32_t v = 0;
-#pragma unroll 4
-			for (int k = 0; k < m; ++k) {
-				const int32_t vm = max(v, F[k]);
-				v = vm + pt[k * ld + j];
-				VW16[(k * xvs + i) * 4 + 0] = uint16_t(vm);
-				VW16[(k * xvs + i) * 4 + 2] = uint16_t(v);
-			}
-		}
-	} else if (warp == 1) {
-		int32_t Gq = 0;
-		const int nj = n - l2;
-		int32_t add = (lane < m && lane == 0 && nj > 0) ? pt[(m - 1) * ld + fr[n - 1]] : 0;
-		for (int s = 0; s < nj + m - 1; ++s) {
-			const int i = s - lane, i1 = i + 1;
-			const int32_t next =
-			    (lane < m && i1 >= 0 && i1 < nj) ? pt[(m - 1 - lane) * ld + fr[n - 1 - i1]] : 0;
-			const int32_t left = __shfl_up_sync(0xffffffffu, Gq, 1);
-			if (lane < m && i >= 0 && i < nj)
-				Gq = max(Gq, lane > 0 ? left : 0) + add;
-			add = next;
-		}
-		if (lane < m)
-			G[lane] = Gq;
-		__syncwarp();
-		for (int i = lane; i < u; i += 32) {
-			const int j = fr[l1 + 1 + i];
-			int32_t g = 0;
-#pragma unroll 4
-			for (int q = 0; q < m; ++q) {
-				const int k = m - 1 - q;
-				const int32_t wm = max(g, G[q]);
-				g = wm + pt[k * ld + j];
-				VW16[(k * xvs + i) * 4 + 1] = uint16_t(wm);
-				VW16[(k * xvs + i) * 4 + 3] = uint16_t(g);
-			}
-		}
-	}
-}
-
-constexpr int kSB = 4; // staged walks and sweep: entries loaded ahead per batch
-
-// One CTA bounds one father at a time; while its walkers run the backward
-// passes, warps 0-1 (idle then) claim the CTA's father after next and load
-// the next father's record into the other record buffer, so neither the
-// claim's round trip nor the record load sits between two fathers. Five
-// barriers per father: record ready, free-job columns, forward passes and
-// fronts, backward passes, children's bounds.
+// The staged form (family_staged.cuh), launched on its own: CTAs take
+// fathers from the device counter after their first (blockIdx.x).
 template <bool kWide>
-__global__ void __launch_bounds__(kFamThreads, 2)
+__global__ void __launch_bounds__(staged::kFamThreads, 2)
     family_staged_kernel(FamilyArgs A, BoundParams bp, const uint32_t *__restrict__ tpack,
-                         const uint8_t *__restrict__ jobposT, StagedLayout L)
+                         const uint8_t *__restrict__ jobposT, staged::StagedLayout L)
 {
-	constexpr int NW = kWide ? 4 : 2; // 32-bit words of a job or position mask
 	extern __shared__ __align__(16) uint8_t smem[];
 	const long long nf = A.count_dev ? *A.count_dev : A.count;
 	if ((long long)blockIdx.x >= nf)
 		return;
-	const int n = bp.n, m = bp.m, P = bp.P, Pp = L.Pp, xcs = L.xcs, xvs = L.xvs;
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	uint32_t *sT = reinterpret_cast<uint32_t *>(smem + L.off_T);
-	uint16_t *sXr = reinterpret_cast<uint16_t *>(smem + L.off_Xr);
-	uint32_t *sRed = reinterpret_cast<uint32_t *>(smem + L.off_Xr);
-	uint8_t *sXq = smem + L.off_Xq;
-	uint16_t *sXc = reinterpret_cast<uint16_t *>(smem + L.off_Xc);
-	uint16_t *sVW16 = reinterpret_cast<uint16_t *>(smem + L.off_VW);
-	const uint2 *sVW = reinterpret_cast<const uint2 *>(smem + L.off_VW);
-	uint4 *sPK = reinterpret_cast<uint4 *>(smem + L.off_PK);
-	int32_t *sHT = reinterpret_cast<int32_t *>(smem + L.off_HT); // heads[32], tails[32]
-	uint16_t *sPt = reinterpret_cast<uint16_t *>(smem + L.off_pt);
-	int32_t *sPairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
-	int32_t *sF = reinterpret_cast<int32_t *>(smem + L.off_F);
-	int32_t *sG = reinterpret_cast<int32_t *>(smem + L.off_G);
-	int16_t *sFrBuf = reinterpret_cast<int16_t *>(smem + L.off_fr); // [2][L.frs]
-	uint8_t *sFidx = smem + L.off_fidx;
-	uint32_t *sMaskBuf = reinterpret_cast<uint32_t *>(smem + L.off_misc); // [2][4]
-	long long *sNext = reinterpret_cast<long long *>(smem + L.off_misc + 32); // [2]
-	const uint8_t *tb = bp.t8.blob;
-
-	// the father that follows the CTA's current one (claimed from the
-	// device counter, or every gridDim.x-th without one)
-	auto claim = [&](long long after) -> long long {
-		return A.next ? (long long)gridDim.x + (long long)atomicAdd(A.next, 1ull)
-		              : after + gridDim.x;
-	};
-	// record of father g into buffer b; job ids clamped to [0, n): a
-	// malformed record gives wrong bounds, never an access outside the
-	// tables. Threads t0 .. t0 + nt - 1.
-	auto load_record = [&](long long g, int b, int t0, int nt) {
-		if (g >= nf)
-			return;
-		const long long ri = A.ridx ? A.ridx[g] : g;
-		const int16_t *g_fr = reinterpret_cast<const int16_t *>(A.fathers + ri * A.stride);
-		int16_t *dst = sFrBuf + b * L.frs;
-		for (int i = tid - t0; i < n + 2; i += nt)
-			dst[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
-	};
-	{
-		const uint4 *src = reinterpret_cast<const uint4 *>(tpack);
-		uint4 *dst = reinterpret_cast<uint4 *>(sT);
-		const int words = n * Pp / 4;
-		for (int i = tid; i < words; i += kFamThreads)
-			dst[i] = __ldg(src + i);
-		const int32_t *g_pt = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pt);
-		const int32_t *g_pairs = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pairs);
-		const int32_t *g_heads = reinterpret_cast<const int32_t *>(tb + bp.t8.off_heads);
-		const int32_t *g_tails = reinterpret_cast<const int32_t *>(tb + bp.t8.off_tails);
-		for (int i = tid; i < m * n; i += kFamThreads)
-			sPt[(i / n) * (n + 1) + i % n] = uint16_t(g_pt[i]);
-		for (int i = tid; i < P; i += kFamThreads)
-			sPairs[i] = g_pairs[i];
-		if (tid < m) {
-			sHT[tid] = g_heads[tid];
-			sHT[32 + tid] = g_tails[tid];
-		}
-		if (tid < 8)
-			sMaskBuf[tid] = 0;
-		if (tid == 0)
-			sNext[0] = claim(blockIdx.x);
-		load_record(blockIdx.x, 0, 0, kFamThreads);
-	}
-	const int t = tid - kFrontThreads; // walker: pair t
-	const bool walker = t >= 0 && t < P;
-	int cur = 0;
-	for (long long f = blockIdx.x; f < nf;) {
-		__syncthreads(); // record f in buffer cur, its successor in sNext[cur]
-		const long long fn = sNext[cur];
-		const int16_t *sFr = sFrBuf + cur * L.frs;
-		uint32_t *sMask = sMaskBuf + 4 * cur;
-		const int l1 = sFr[n], l2 = sFr[n + 1];
-		const int u = l2 - l1 - 1;
-		const long long c0 = A.child_off[f];
-		// the next record and the claim after it, by warps 0-1 while they
-		// have nothing else to do
-		auto prefetch = [&]() {
-			if (tid < kFrontThreads) {
-				if (tid == 0)
-					sNext[cur ^ 1] = fn < nf ? claim(fn) : nf;
-				load_record(fn, cur ^ 1, 0, kFrontThreads);
-			}
-		};
-		// cursors outside -1 <= l1, l2 <= n with two free jobs or more, or a
-		// child range of another size: the father is skipped
-		// (every path clears the other job mask, its father's being done)
-		if (l1 < -1 || l2 > n || u < 2 || A.child_off[f + 1] - c0 != (u == 2 ? 2 : 2 * u)) {
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
-			prefetch();
-			f = fn;
-			cur ^= 1;
-			continue;
-		}
-		if (u == 2) {
-			// two leaves: makespans of front + (x, y) + back, both orders
-			FamSmem S2{};
-			S2.pt = sPt;
-			S2.fr = const_cast<int16_t *>(sFr);
-			S2.F = sF;
-			S2.G = sG;
-			fronts_and_backs(S2, warp, lane, n, m, P, l1, l2, u, sHT, sHT + 32, true);
-			__syncthreads();
-			if (tid < 2) {
-				const int x = sFr[l1 + 1 + tid], y = sFr[l1 + 2 - tid];
-				int32_t v1 = 0, v2 = 0, mk = 0;
-				for (int k = 0; k < m; ++k) {
-					v1 = max(v1, sF[k]) + sPt[k * (n + 1) + x];
-					v2 = max(v2, v1) + sPt[k * (n + 1) + y];
-					mk = max(mk, v2 + sG[m - 1 - k]);
-				}
-				A.child_lb[c0 + tid] = mk;
-				A.child_job[c0 + tid] = int16_t(x);
-			}
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
-			prefetch();
-			f = fn;
-			cur ^= 1;
-			continue;
-		}
-		// free jobs: their columns and the job mask
-		if (tid < u) {
-			const int j = sFr[l1 + 1 + tid];
-			sFidx[j] = uint8_t(tid);
-			atomicOr(&sMask[j >> 5], 1u << (j & 31));
-		}
-		__syncthreads();
-		// a record whose free jobs repeat one another is skipped (its walks
-		// would find fewer than u positions)
-		if (__popc(sMask[0]) + __popc(sMask[1]) + __popc(sMask[2]) + __popc(sMask[3]) != u) {
-			__syncthreads(); // every thread has read the mask
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
-			prefetch();
-			f = fn;
-			cur ^= 1;
-			continue;
-		}
-		// walks: scan all n positions when most jobs are free (more than
-		// 3/4), else follow the position table over the free ones only
-		const bool scan = 4 * u > 3 * n;
-		int32_t Asum = 0, Bsum = 0;
-		if (walker) {
-			int32_t c = kNeg, as = 0, bs = 0;
-			if (scan) {
-				uint32_t w[NW];
-#pragma unroll
-				for (int i = 0; i < NW; ++i)
-					w[i] = sMask[i];
-				int k = 0;
-				for (int q0 = 0; q0 < n; q0 += kSB) {
-					uint32_t e[kSB];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						e[j] = q0 + j < n ? sT[(q0 + j) * Pp + t] : 0u;
-#pragma unroll
-					for (int j = 0; j < kSB; ++j) {
-						if (q0 + j < n && mask_has<NW>(w, int(e[j] & 127u))) {
-							sXr[k * Pp + t] = uint16_t(c);
-							const int32_t a = int32_t((e[j] >> 7) & 127u);
-							const int32_t b = int32_t((e[j] >> 14) & 127u);
-							c = max(c + b, as + int32_t(e[j] >> 21));
-							as += a;
-							bs += b;
-							++k;
-						}
-					}
-				}
-			} else {
-				uint32_t w[NW];
-#pragma unroll
-				for (int i = 0; i < NW; ++i)
-					w[i] = 0;
-				const int16_t *fj = sFr + l1 + 1;
-#pragma unroll 4
-				for (int i = 0; i < u; ++i) {
-					const int q = __ldg(jobposT + (size_t)fj[i] * P + t);
-#pragma unroll
-					for (int wi = 0; wi < NW; ++wi)
-						w[wi] |= (q >> 5) == wi ? 1u << (q & 31) : 0u;
-				}
-				// batches of kSB: positions first, then their entries (the
-				// loads in flight together), then the recurrence
-				for (int k0 = 0; k0 < u; k0 += kSB) {
-					int q[kSB];
-					uint32_t e[kSB];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						q[j] = k0 + j < u ? pop_lowest<NW>(w) : 0;
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						e[j] = sT[q[j] * Pp + t];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j) {
-						if (k0 + j < u) {
-							sXq[(k0 + j) * Pp + t] = uint8_t(q[j]);
-							sXr[(k0 + j) * Pp + t] = uint16_t(c);
-							const int32_t a = int32_t((e[j] >> 7) & 127u);
-							const int32_t b = int32_t((e[j] >> 14) & 127u);
-							c = max(c + b, as + int32_t(e[j] >> 21));
-							as += a;
-							bs += b;
-						}
-					}
-				}
-			}
-			Asum = as;
-			Bsum = bs;
-		} else if (tid < kFrontThreads) {
-			staged_fronts(warp, lane, n, m, l1, l2, u, xvs, sPt, sFr, sF, sG, sVW16);
-		}
-		__syncthreads(); // fronts, backs and every forward pass done
-		if (walker) {
-			// the pair's constants for the children's bounds: the father's
-			// front on m1, m2 (the static heads without one) and back (0 on m1
-			// and the static tail on m2 without one)
-			const int pr = sPairs[t], ma = pr & 0xff, mb = pr >> 8;
-			const int32_t f1 = l1 >= 0 ? sF[ma] : sHT[ma], f2 = l1 >= 0 ? sF[mb] : sHT[mb];
-			const int32_t r1 = l2 < n ? sG[m - 1 - ma] : 0;
-			const int32_t r2 = l2 < n ? sG[m - 1 - mb] : sHT[32 + mb];
-			sPK[t] = make_uint4(uint32_t(Bsum + r2) | uint32_t(Bsum + f2) << 16,
-			                    uint32_t(r2) | uint32_t(f1) << 16,
-			                    uint32_t(Asum + r1) | uint32_t(Asum + f1) << 16,
-			                    uint32_t(ma * xvs) | uint32_t(mb * xvs) << 16);
-			// backward: X_j = max(Csuf + Apre, Bsuf + Cpre) at each free job
-			int32_t cs = kNeg, bs = 0, R = Asum; // R = A minus the suffix's a
-			auto step = [&](uint32_t e, int32_t pre, int col) {
-				const int32_t a = int32_t((e >> 7) & 127u), b = int32_t((e >> 14) & 127u);
-				const int32_t x = max(pre + bs, R - a + cs);
-				cs = max(cs + a, bs + int32_t(e >> 21));
-				R -= a;
-				bs += b;
-				sXc[t * xcs + col] = uint16_t(x);
-			};
-			if (scan) {
-				uint32_t w[NW];
-#pragma unroll
-				for (int i = 0; i < NW; ++i)
-					w[i] = sMask[i];
-				int k = u;
-				for (int q0 = n - 1; q0 >= 0; q0 -= kSB) {
-					uint32_t e[kSB];
-					int col[kSB];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						e[j] = q0 - j >= 0 ? sT[(q0 - j) * Pp + t] : 0u;
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						col[j] = sFidx[e[j] & 127u];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						if (q0 - j >= 0 && mask_has<NW>(w, int(e[j] & 127u))) {
-							--k;
-							step(e[j], int32_t(sXr[k * Pp + t]), col[j]);
-						}
-				}
-			} else {
-				for (int k0 = u - 1; k0 >= 0; k0 -= kSB) {
-					int q[kSB], col[kSB];
-					int32_t pre[kSB];
-					uint32_t e[kSB];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j) {
-						const int k = max(k0 - j, 0);
-						q[j] = sXq[k * Pp + t];
-						pre[j] = int32_t(sXr[k * Pp + t]);
-					}
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						e[j] = sT[q[j] * Pp + t];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						col[j] = sFidx[e[j] & 127u];
-#pragma unroll
-					for (int j = 0; j < kSB; ++j)
-						if (k0 - j >= 0)
-							step(e[j], pre[j], col[j]);
-				}
-			}
-		} else {
-			// warps 0-1: clear the other mask buffer (its father is done),
-			// then claim and load ahead
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
-			prefetch();
-		}
-		__syncthreads(); // every X_j and pair constant in place
-		// the children's bounds: thread (column i, slice rs) of NS slices
-		// takes the pairs rs, rs + NS, ...; tid / u without an integer
-		// division ((tid + 1/2) / u lies at least 1/(2u) >= 1/256 from an
-		// integer, far beyond the float error of a quotient below 256)
-		const int rs = int((float(tid) + 0.5f) * __frcp_rn(float(u)));
-		const int NS = min(int((float(kFamThreads) + 0.5f) * __frcp_rn(float(u))), 32);
-		uint32_t acc = 0; // (BEGIN bound | END bound << 16)
-		if (rs < NS) {
-			const int i = tid - rs * u;
-			for (int p0 = rs; p0 < P; p0 += kSB * NS) {
-				uint4 pk[kSB];
-				uint32_t x[kSB];
-				uint2 e1[kSB], e2[kSB];
-#pragma unroll
-				for (int j = 0; j < kSB; ++j) {
-					const int p = min(p0 + j * NS, P - 1);
-					pk[j] = sPK[p];
-					x[j] = sXc[p * xcs + i];
-				}
-#pragma unroll
-				for (int j = 0; j < kSB; ++j) {
-					e1[j] = sVW[(pk[j].w & 0xffffu) + i];
-					e2[j] = sVW[(pk[j].w >> 16) + i];
-				}
-				// a repeated last pair (past P) only repeats a maximum
-#pragma unroll
-				for (int j = 0; j < kSB; ++j) {
-					const uint32_t T1 = e2[j].x + pk[j].x;
-					const uint32_t T3 = e1[j].x + pk[j].z;
-					const uint32_t T2 =
-					    __byte_perm(e1[j].y, e2[j].y, 0x7610) + x[j] * 0x10001u + pk[j].y;
-					acc = __vmaxu2(acc, __vimax3_u16x2(T1, T2, T3));
-				}
-			}
-		}
-		sRed[tid] = acc; // Xr is consumed
-		__syncthreads();
-		if (tid < u) {
-			uint32_t r = sRed[tid];
-			for (int k = 1; k < NS; ++k)
-				r = __vmaxu2(r, sRed[k * u + tid]);
-			const int16_t job = sFr[l1 + 1 + tid];
-			A.child_job[c0 + tid] = job;
-			A.child_job[c0 + u + tid] = job;
-			A.child_lb[c0 + tid] = int32_t(r & 0xffffu);
-			A.child_lb[c0 + u + tid] = int32_t(r >> 16);
-		}
-		f = fn;
-		cur ^= 1;
-	}
+	staged::staged_load_tables(bp, tpack, L, smem);
+	staged::staged_fathers<kWide>(A, bp, jobposT, L, smem, nf, (long long)blockIdx.x,
+	                              [&](long long after) -> long long {
+		                              return A.next ? (long long)gridDim.x +
+		                                                  (long long)atomicAdd(A.next, 1ull)
+		                                            : after + gridDim.x;
+	                              });
 }
 
 }  // namespace
@@ -1236,7 +733,7 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, cons
 	const bool learned = A.fpairs != nullptr;
 	const bool wide = bp.n > 64;
 	if (!learned && T.tpack && p16 && bp.P <= kWalkThreads && smem_kb <= 0) {
-		const StagedLayout SL = staged_layout(bp.n, bp.m, bp.P, T.Pp);
+		const staged::StagedLayout SL = staged::staged_layout(bp.n, bp.m, bp.P, T.Pp);
 		int dev = 0, max_optin = 0;
 		cudaError_t e = cudaGetDevice(&dev);
 		if (e == cudaSuccess)
@@ -1245,7 +742,7 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, cons
 			return e;
 		if (SL.bytes + 1024 <= size_t(max_optin)) {
 			using SKern = void (*)(FamilyArgs, BoundParams, const uint32_t *, const uint8_t *,
-			                       StagedLayout);
+			                       staged::StagedLayout);
 			const SKern sk = wide ? family_staged_kernel<true> : family_staged_kernel<false>;
 			e = allow_max_dynamic_smem(sk);
 			int occ = 0;

@@ -41,6 +41,11 @@ class ExploreStats(C.Structure):
 NO_GRAPH = 1
 CHILD_LB2 = 2  # bound every child record on its own instead of per father (same bounds)
 RESUME = 4     # continue the context's stopped or seeded search
+RESIDENT = 8   # run as the resident search (one cooperative launch)
+
+
+class ResidentOpts(C.Structure):
+    _fields_ = [("wait_ms", C.c_int32), ("self_test", C.c_int32)]
 
 
 def coverage(hist, n: int) -> int:
@@ -58,7 +63,7 @@ def _cfg(ub0, best, window, graph_iters, capacity, max_iters, flags, family_smem
 def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int = 0,
             graph_iters: int = 0, capacity: int = 0, max_iters: int = 0, graph: bool = True,
             stream: int = 0, child_lb2: bool = False, family_smem_kb: int = 0,
-            max_bounded: int = 0, resume: bool = False) -> dict:
+            max_bounded: int = 0, resume: bool = False, resident: bool = False) -> dict:
     """The exact GPU search. `child_lb2` bounds each child record on its own
     with the per-node LB2 kernel (the reference GPU kernel's form) instead of
     each father's children together; bounds and tree are the same.
@@ -68,7 +73,7 @@ def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int
     L = lib()
     L.wsbb_explore.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     flags = (0 if graph else NO_GRAPH) | (CHILD_LB2 if child_lb2 else 0) | \
-        (RESUME if resume else 0)
+        (RESUME if resume else 0) | (RESIDENT if resident else 0)
     cfg = _cfg(ub0, best, window, graph_iters, capacity, max_iters, flags, family_smem_kb,
                max_bounded)
     st = ExploreStats()
@@ -76,6 +81,38 @@ def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int
     if rc != 0:
         raise WsbbError(rc, L.wsbb_last_error(ctx.h).decode())
     return stats_dict(st, ctx.n)
+
+
+def explore_resident(ctxs, ub0s=None, bests=None, window: int = 0, capacity: int = 0,
+                     max_iters: int = 0, max_bounded=0, wait_ms: int = 0,
+                     self_test: bool = False, stream: int = 0, check: bool = True):
+    """Search every context's instance in one launch of resident CTAs
+    (wsbb_explore_resident): a group of CTAs per instance, fathers stolen
+    between CTAs and from instances still running. `ub0s`, `bests`,
+    `capacity`, `max_iters` and `max_bounded` may be one value for all or
+    one per context. Returns
+    (return code, [stats dict per instance]); with `check`, a failure
+    raises."""
+    L = lib()
+    L.wsbb_explore_resident.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]
+    k = len(ctxs)
+
+    def per(v, default):
+        if v is None:
+            return [default] * k
+        return list(v) if isinstance(v, (list, tuple)) else [v] * k
+    u, b, mb = per(ub0s, None), per(bests, 99999), per(max_bounded, 0)
+    cap, mi = per(capacity, 0), per(max_iters, 0)
+    cfgs = (ExploreCfg * k)(*[_cfg(u[i], b[i], window, 0, cap[i], mi[i], 0, 0, mb[i])
+                              for i in range(k)])
+    hs = (C.c_void_p * k)(*[c.h for c in ctxs])
+    st = (ExploreStats * k)()
+    opts = ResidentOpts(int(wait_ms), 1 if self_test else 0)
+    rc = L.wsbb_explore_resident(hs, k, cfgs, C.byref(opts), st, stream or None)
+    if rc != 0 and check:
+        raise WsbbError(rc, L.wsbb_last_error(ctxs[0].h).decode())
+    return rc, [stats_dict(st[i], ctxs[i].n) for i in range(k)]
 
 
 def explore_seed(ctx: Context, records: np.ndarray, lbs, ub0: int | None = None,
