@@ -398,12 +398,21 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 				for (int i = 0; i < NW; ++i)
 					w[i] = 0;
 				const int16_t *fj = sFr + l1 + 1;
+				if (NW == 2) { // n <= 64: one 64-bit word
+					uint64_t m64 = 0;
 #pragma unroll 4
-				for (int i = 0; i < u; ++i) {
-					const int q = __ldg(jobposT + (size_t)fj[i] * P + t);
+					for (int i = 0; i < u; ++i)
+						m64 |= 1ull << __ldg(jobposT + (size_t)fj[i] * P + t);
+					w[0] = uint32_t(m64);
+					w[NW - 1] = uint32_t(m64 >> 32);
+				} else {
+#pragma unroll 4
+					for (int i = 0; i < u; ++i) {
+						const int q = __ldg(jobposT + (size_t)fj[i] * P + t);
 #pragma unroll
-					for (int wi = 0; wi < NW; ++wi)
-						w[wi] |= (q >> 5) == wi ? 1u << (q & 31) : 0u;
+						for (int wi = 0; wi < NW; ++wi)
+							w[wi] |= (q >> 5) == wi ? 1u << (q & 31) : 0u;
+					}
 				}
 				// batches of kSB: positions first, then their entries (the
 				// loads in flight together), then the recurrence
