@@ -62,6 +62,9 @@ TREE_KEYS = ("branched", "pruned", "leaves", "improved", "bounded", "best_cost",
 KERNELS_PER_ITER = 11
 
 POOL_N, POOL_M, POOL, POOL_SEEDS, LEAF_SHARE = 20, 20, 1 << 20, 10, 0.02
+# DRAM bytes (read + write) of one roofline launch of the family kernel, from
+# the ncu capture summarised in profiles/family_kernel_n50m20.md
+FAMILY_DRAM_BYTES_PER_LAUNCH = 4.05e6
 PROOF_N, PROOF_M, PROOF_SEEDS = 50, 10, (0, 1, 2, 3, 4)
 
 
@@ -252,15 +255,22 @@ def roofline_family(ctx, dev, stream, sptr, peak) -> dict:
     bytes_ = recs.nbytes + off.nbytes + int(off[-1]) * 6
     return {"bound": "int32", "achieved": achieved / 1e12,
             "peak": peak / 1e12 if peak else None, "unit": "Tops/s",
-            "frac": achieved / peak if peak else None, "traffic": None,
-            "kernel": "family_kernel (wsbb_decompose_lb2)",
+            "frac": achieved / peak if peak else None,
+            "traffic": FAMILY_DRAM_BYTES_PER_LAUNCH,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of this launch, "
+                              "one ncu capture (profiles/family_kernel_n50m20.md): the tables "
+                              "and records stay in L2, far below the algorithmic bytes",
+            "algorithmic_bytes": bytes_,
+            "peak_note": "the probe's chains issue one thread instruction per counted "
+                         "operation (a subtraction and a fused add+max: two operations, two "
+                         "instructions) at ~98 % of the SMs' issue rate; the algorithmic "
+                         "count counts an add and a max as two operations too",
+            "kernel": "family_staged_kernel (wsbb_decompose_lb2)",
             "workload": f"{count} fathers n={S_N} m={S_M}, u uniform in [3, {S_N}]",
             "launch_ms": t * 1e3, "ops_per_launch": ops,
             "peak_source": "measured in this run: add+max chains on every SM "
                            "(wsbb_probe_maxplus_peak)",
-            "hbm_achieved_gbs": bytes_ / t / 1e9,
-            "traffic_note": "DRAM traffic per launch is in the committed ncu summary: "
-                            "the kernel's tables stay in L2"}
+            "hbm_achieved_gbs": bytes_ / t / 1e9}
 
 
 def lb2_pool_section(dev, stream, sptr, peak, launches: int) -> dict:
