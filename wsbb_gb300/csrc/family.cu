@@ -694,10 +694,11 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 	}
 }
 
-// The staged form (family_staged.cuh), launched on its own: CTAs take
-// fathers from the device counter after their first (blockIdx.x).
-template <bool kWide>
-__global__ void __launch_bounds__(staged::kFamThreads, 2)
+// The staged form (family_staged.cuh), launched on its own: CTAs of NT
+// threads take fathers from the device counter after their first
+// (blockIdx.x).
+template <bool kWide, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT)
     family_staged_kernel(FamilyArgs A, BoundParams bp, const uint32_t *__restrict__ tpack,
                          const uint8_t *__restrict__ jobposT, staged::StagedLayout L)
 {
@@ -706,7 +707,7 @@ __global__ void __launch_bounds__(staged::kFamThreads, 2)
 	if ((long long)blockIdx.x >= nf)
 		return;
 	staged::staged_load_tables(bp, tpack, L, smem);
-	staged::staged_fathers<kWide>(A, bp, jobposT, L, smem, nf, (long long)blockIdx.x,
+	staged::staged_fathers<kWide, NT>(A, bp, jobposT, L, smem, nf, (long long)blockIdx.x,
 	                              [&](long long after) -> long long {
 		                              return A.next ? (long long)gridDim.x +
 		                                                  (long long)atomicAdd(A.next, 1ull)
@@ -743,16 +744,22 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, cons
 		if (SL.bytes + 1024 <= size_t(max_optin)) {
 			using SKern = void (*)(FamilyArgs, BoundParams, const uint32_t *, const uint8_t *,
 			                       staged::StagedLayout);
-			const SKern sk = wide ? family_staged_kernel<true> : family_staged_kernel<false>;
+			// up to 64 pairs: CTAs of 128 threads (more of them per SM)
+			const bool small = bp.P <= staged::kFamThreadsSmall - staged::kFrontThreads;
+			const int nt = small ? staged::kFamThreadsSmall : staged::kFamThreads;
+			const SKern sk = small ? (wide ? family_staged_kernel<true, staged::kFamThreadsSmall>
+			                               : family_staged_kernel<false, staged::kFamThreadsSmall>)
+			                       : (wide ? family_staged_kernel<true, staged::kFamThreads>
+			                               : family_staged_kernel<false, staged::kFamThreads>);
 			e = allow_max_dynamic_smem(sk);
 			int occ = 0;
 			if (e == cudaSuccess)
-				e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sk, kFamThreads, SL.bytes);
+				e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sk, nt, SL.bytes);
 			if (e != cudaSuccess)
 				return e;
 			const long long grid =
 			    std::min<long long>(max_fathers, (long long)num_sms * std::max(occ, 1));
-			sk<<<unsigned(grid), kFamThreads, SL.bytes, s>>>(A, bp, T.tpack, T.jobposT, SL);
+			sk<<<unsigned(grid), nt, SL.bytes, s>>>(A, bp, T.tpack, T.jobposT, SL);
 			return cudaGetLastError();
 		}
 	}

@@ -11,8 +11,11 @@
 namespace wsbb {
 namespace staged {
 
+// CTAs of kFamThreads (P > 64 pairs) or kFamThreadsSmall (P <= 64, more
+// CTAs per SM): warps 0-1 compute fronts and backs, the rest walk pairs
 constexpr int kFamThreads = 256;
-constexpr int kFrontThreads = 64; // warps 0-1: fronts and backs, while the rest walk pairs
+constexpr int kFamThreadsSmall = 128;
+constexpr int kFrontThreads = 64;
 constexpr int kWalkThreads = kFamThreads - kFrontThreads;
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
@@ -210,7 +213,7 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 	const uint4 *src = reinterpret_cast<const uint4 *>(tpack);
 	uint4 *dst = reinterpret_cast<uint4 *>(smem + L.off_T);
 	const int words = n * L.Pp / 4;
-	for (int i = tid; i < words; i += kFamThreads)
+	for (int i = tid; i < words; i += int(blockDim.x))
 		dst[i] = __ldg(src + i);
 	const uint8_t *tb = bp.t8.blob;
 	const int32_t *g_pt = reinterpret_cast<const int32_t *>(tb + bp.t8.off_pt);
@@ -220,9 +223,9 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 	uint16_t *sPt = reinterpret_cast<uint16_t *>(smem + L.off_pt);
 	int32_t *sPairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
 	int32_t *sHT = reinterpret_cast<int32_t *>(smem + L.off_HT);
-	for (int i = tid; i < m * n; i += kFamThreads)
+	for (int i = tid; i < m * n; i += int(blockDim.x))
 		sPt[(i / n) * (n + 1) + i % n] = uint16_t(g_pt[i]);
-	for (int i = tid; i < P; i += kFamThreads)
+	for (int i = tid; i < P; i += int(blockDim.x))
 		sPairs[i] = g_pairs[i];
 	if (tid < m) {
 		sHT[tid] = g_heads[tid];
@@ -239,9 +242,10 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 //
 // staged_fathers bounds the fathers first, claim(first), claim(that), ...
 // until a claim returns nf or more, with the tables already staged
-// (staged_load_tables, followed by any barrier); every thread of the CTA
-// calls it with the same arguments. Returns the number of fathers it bounded.
-template <bool kWide, typename Claim>
+// (staged_load_tables, followed by any barrier); every thread of a CTA of
+// NT threads (P <= NT - 64) calls it with the same arguments. Returns the
+// number of fathers it bounded.
+template <bool kWide, int NT, typename Claim>
 __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
                                     const uint8_t *__restrict__ jobposT, const StagedLayout &L,
                                     uint8_t *smem, long long nf, long long first, Claim claim)
@@ -283,7 +287,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		sMaskBuf[tid] = 0;
 	if (tid == 0)
 		sNext[0] = first < nf ? claim(first) : nf;
-	load_record(first, 0, 0, kFamThreads);
+	load_record(first, 0, 0, NT);
 	long long done = 0;
 	const int t = tid - kFrontThreads; // walker: pair t
 	const bool walker = t >= 0 && t < P;
@@ -497,7 +501,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		// division ((tid + 1/2) / u lies at least 1/(2u) >= 1/256 from an
 		// integer, far beyond the float error of a quotient below 256)
 		const int rs = int((float(tid) + 0.5f) * __frcp_rn(float(u)));
-		const int NS = min(int((float(kFamThreads) + 0.5f) * __frcp_rn(float(u))), 32);
+		const int NS = min(int((float(NT) + 0.5f) * __frcp_rn(float(u))), 32);
 		uint32_t acc = 0; // (BEGIN bound | END bound << 16)
 		if (rs < NS) {
 			const int i = tid - rs * u;

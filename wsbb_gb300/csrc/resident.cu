@@ -195,8 +195,10 @@ __device__ void bound_phase(const ResInst &I, unsigned long long ph, int own, ui
 		return; // uniform
 	auto claim = [&](long long) { return claim_father(I, ph, own); };
 	const long long done =
-	    I.wide ? staged::staged_fathers<true>(I.FA, I.bp, I.jobposT, I.L, smem, nf, first, claim)
-	           : staged::staged_fathers<false>(I.FA, I.bp, I.jobposT, I.L, smem, nf, first, claim);
+	    I.wide ? staged::staged_fathers<true, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, nf,
+	                                                       first, claim)
+	           : staged::staged_fathers<false, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, nf,
+	                                                        first, claim);
 	__threadfence(); // the CTA's child bounds, before they are counted
 	__syncthreads();
 	if (threadIdx.x == 0)
@@ -524,7 +526,7 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 	for (int k = 0; k < count && e == cudaSuccess; ++k) {
 		ExploreState *X = ctxs[k]->ex;
 		init_kernel<<<1, 128, 0, s>>>(X->P, cfgs[k].ub0, cfgs[k].best, window_min_of(X->window),
-		                              X->window);
+		                              X->window, cfgs[k].max_iters > 0 || cfgs[k].max_bounded > 0);
 		e = cudaGetLastError();
 	}
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
