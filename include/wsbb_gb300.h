@@ -207,7 +207,10 @@ typedef struct {
 	 * (pending_hist: by their depth), so the sequential search's counters
 	 * after exactly `takes` takes (nodes popped: branched + pruned + leaves
 	 * - pending) are these counters with pruned - pending and depth_hist -
-	 * pending_hist. Both are 0 once the search completes. */
+	 * pending_hist. Both are 0 once the search completes. The accounting
+	 * runs for searches that may stop early — started with max_iters or
+	 * max_bounded, or seeded; a search started without either runs to its
+	 * end and reports pending = 0. */
 	int64_t takes;
 	int64_t pending;
 	uint32_t pending_hist[WSBB_MAX_JOBS + 1];

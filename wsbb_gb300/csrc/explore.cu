@@ -336,7 +336,8 @@ int run_search(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, const SearchMode &M, 
 	if (resume)
 		resume_kernel<<<1, 32, 0, s>>>(X->P, cfg->ub0, cfg->best);
 	else
-		init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window);
+		init_kernel<<<1, 128, 0, s>>>(X->P, cfg->ub0, cfg->best, window_min_of(window), window,
+		                              cfg->max_iters > 0 || cfg->max_bounded > 0);
 	e = cudaGetLastError();
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "search init");
@@ -683,7 +684,8 @@ extern "C" int wsbb_explore_noalloc(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg,
 	if (!stream_v && (e = wait_for_legacy(s, ctx->legacy_ev)) != cudaSuccess)
 		return ex_fail(ctx, e, "stream ordering");
 	const auto t0 = std::chrono::steady_clock::now();
-	init_kernel<<<1, 128, 0, s>>>(X.P, cfg->ub0, cfg->best, window_min_of(window), window);
+	init_kernel<<<1, 128, 0, s>>>(X.P, cfg->ub0, cfg->best, window_min_of(window), window,
+	                              cfg->max_iters > 0 || cfg->max_bounded > 0);
 	e = cudaGetLastError();
 	if (e != cudaSuccess)
 		return ex_fail(ctx, e, "search init");

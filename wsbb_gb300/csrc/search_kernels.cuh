@@ -68,6 +68,11 @@ struct ExDev {
 	// father's block closes; a stopped search subtracts them to report the
 	// exact sequential prefix.
 	unsigned pend[WSBB_MAX_JOBS + 1];
+	// 1: keep pend (a search that may stop before it completes: an
+	// iteration or node budget, or a seeded search); 0: a search that runs
+	// to its end, where nothing is pending at the end and commit skips the
+	// accounting
+	int track_pend;
 };
 
 struct ExParams {
@@ -307,6 +312,7 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 
 	long long top = D->top;
 	const int ub0 = D->ub;
+	const bool track = D->track_pend != 0;
 	int ub = ub0;
 	unsigned long long c_br = 0, c_pr = 0, c_lf = 0, c_im = 0, c_bd = 0, c_dead = 0;
 
@@ -401,14 +407,15 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 				P.best_rec[b] = P.rec[src * P.stride + b];
 			ub = cmin;
 		}
-		// Open blocks. A committed entry of depth e closes the block of every
+		// Open blocks (only for a search that may stop early). A committed
+		// entry of depth e closes the block of every
 		// father of depth >= e (the sequential search has taken that
 		// father's pruned-at-birth children just before it); a committed
 		// marker opens its own. After the round, pend[d] for d >= the
 		// round's smallest depth belongs to the last entry of depth <= d:
 		// its npruned if it has depth d and is a marker, else 0. Those last
 		// entries are the round's suffix minima of depth (distinct depths).
-		{
+		if (track) {
 			int loc_min = INT_MAX;
 			bool has_np = false;
 #pragma unroll
@@ -1082,12 +1089,14 @@ __device__ __forceinline__ void finish_body(const ExParams &P)
 
 __global__ void finish_iteration_kernel(ExParams P) { finish_body(P); }
 
-__global__ void init_kernel(ExParams P, int ub0, int best, int win_min, int win_max)
+__global__ void init_kernel(ExParams P, int ub0, int best, int win_min, int win_max,
+                            int track_pend)
 {
 	ExDev *D = P.dev;
 	const int n = P.n, S = P.stride;
 	if (threadIdx.x == 0) {
 		memset(D, 0, sizeof(ExDev));
+		D->track_pend = track_pend;
 		D->top = 0;
 		D->ub = ub0;
 		D->best = best;
@@ -1122,6 +1131,7 @@ __global__ void seed_kernel(ExParams P, long long count, int ub0, int best, int 
 	const int n = P.n, S = P.stride;
 	if (threadIdx.x == 0) {
 		memset(D, 0, sizeof(ExDev));
+		D->track_pend = 1;
 		D->top = count - 1;
 		D->done = count == 0;
 		D->ub = ub0;
