@@ -694,25 +694,30 @@ __global__ void __launch_bounds__(kFamThreads, 4) family_kernel(FamilyArgs A, Bo
 	}
 }
 
-// The staged form (family_staged.cuh), launched on its own: CTAs of NT
-// threads take fathers from the device counter after their first
-// (blockIdx.x).
+// The staged form (family_staged.cuh), launched on its own: CTAs of
+// L.groups groups of NT threads over one copy of the tables; group g of CTA
+// b starts with father g * gridDim.x + b (a batch smaller than the grid
+// spreads over the SMs) and takes the next ones from the device counter.
 template <bool kWide, int NT>
-__global__ void __launch_bounds__(NT, 512 / NT)
+__global__ void __launch_bounds__(staged::kMaxCtaThreads, 1)
     family_staged_kernel(FamilyArgs A, BoundParams bp, const uint32_t *__restrict__ tpack,
                          const uint8_t *__restrict__ jobposT, staged::StagedLayout L)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
 	const long long nf = A.count_dev ? *A.count_dev : A.count;
+	const long long groups = L.groups;
 	if ((long long)blockIdx.x >= nf)
 		return;
 	staged::staged_load_tables(bp, tpack, L, smem);
-	staged::staged_fathers<kWide, NT>(A, bp, jobposT, L, smem, nf, (long long)blockIdx.x,
-	                              [&](long long after) -> long long {
-		                              return A.next ? (long long)gridDim.x +
-		                                                  (long long)atomicAdd(A.next, 1ull)
-		                                            : after + gridDim.x;
-	                              });
+	__syncthreads();
+	const int group = int(threadIdx.x) / NT;
+	const long long base = (long long)gridDim.x * groups;
+	staged::staged_fathers<kWide, NT>(A, bp, jobposT, L, smem, group, nf,
+	                                  (long long)group * gridDim.x + blockIdx.x,
+	                                  [&](long long after) -> long long {
+		                                  return A.next ? base + (long long)atomicAdd(A.next, 1ull)
+		                                                : after + base;
+	                                  });
 }
 
 }  // namespace
@@ -734,19 +739,23 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, cons
 	const bool learned = A.fpairs != nullptr;
 	const bool wide = bp.n > 64;
 	if (!learned && T.tpack && p16 && bp.P <= kWalkThreads && smem_kb <= 0) {
-		const staged::StagedLayout SL = staged::staged_layout(bp.n, bp.m, bp.P, T.Pp);
 		int dev = 0, max_optin = 0;
 		cudaError_t e = cudaGetDevice(&dev);
 		if (e == cudaSuccess)
 			e = cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
 		if (e != cudaSuccess)
 			return e;
+		// up to 64 pairs: groups of 128 threads; as many groups per CTA as
+		// its shared memory and kMaxCtaThreads allow
+		const bool small = bp.P <= staged::kFamThreadsSmall - staged::kFrontThreads;
+		const int nt = small ? staged::kFamThreadsSmall : staged::kFamThreads;
+		int groups = staged::kMaxCtaThreads / nt;
+		staged::StagedLayout SL = staged::staged_layout(bp.n, bp.m, bp.P, T.Pp, groups);
+		while (groups > 1 && SL.bytes + 1024 > size_t(max_optin))
+			SL = staged::staged_layout(bp.n, bp.m, bp.P, T.Pp, --groups);
 		if (SL.bytes + 1024 <= size_t(max_optin)) {
 			using SKern = void (*)(FamilyArgs, BoundParams, const uint32_t *, const uint8_t *,
 			                       staged::StagedLayout);
-			// up to 64 pairs: CTAs of 128 threads (more of them per SM)
-			const bool small = bp.P <= staged::kFamThreadsSmall - staged::kFrontThreads;
-			const int nt = small ? staged::kFamThreadsSmall : staged::kFamThreads;
 			const SKern sk = small ? (wide ? family_staged_kernel<true, staged::kFamThreadsSmall>
 			                               : family_staged_kernel<false, staged::kFamThreadsSmall>)
 			                       : (wide ? family_staged_kernel<true, staged::kFamThreads>
@@ -754,12 +763,12 @@ cudaError_t launch_family_lb2(const BoundParams &bp, const DeviceTables &T, cons
 			e = allow_max_dynamic_smem(sk);
 			int occ = 0;
 			if (e == cudaSuccess)
-				e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sk, nt, SL.bytes);
+				e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, sk, nt * groups, SL.bytes);
 			if (e != cudaSuccess)
 				return e;
-			const long long grid =
-			    std::min<long long>(max_fathers, (long long)num_sms * std::max(occ, 1));
-			sk<<<unsigned(grid), nt, SL.bytes, s>>>(A, bp, T.tpack, T.jobposT, SL);
+			const long long grid = std::min<long long>((max_fathers + groups - 1) / groups,
+			                                           (long long)num_sms * std::max(occ, 1));
+			sk<<<unsigned(grid), nt * groups, SL.bytes, s>>>(A, bp, T.tpack, T.jobposT, SL);
 			return cudaGetLastError();
 		}
 	}

@@ -11,12 +11,16 @@
 namespace wsbb {
 namespace staged {
 
-// CTAs of kFamThreads (P > 64 pairs) or kFamThreadsSmall (P <= 64, more
-// CTAs per SM): warps 0-1 compute fronts and backs, the rest walk pairs
+// Groups of kFamThreads threads (P > 64 pairs) or kFamThreadsSmall (P <=
+// 64): each group bounds its own fathers, two of its warps computing fronts
+// and backs while the rest walk pairs. A CTA holds up to kMaxCtaThreads
+// threads of groups that share one copy of the instance's tables, so that
+// the table is staged once per SM rather than once per father in flight.
 constexpr int kFamThreads = 256;
 constexpr int kFamThreadsSmall = 128;
 constexpr int kFrontThreads = 64;
 constexpr int kWalkThreads = kFamThreads - kFrontThreads;
+constexpr int kMaxCtaThreads = 768;
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
 //// The same bounds, organised around shared memory (plain bounds of fathers
@@ -37,22 +41,35 @@ constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 //    consecutive words, and both children's three terms are computed as
 //    16-bit halves of one word (add, then one three-way and one two-way
 //    unsigned 16-bit maximum).
+// The CTA's tables first (T, heads and tails, processing times, pairs),
+// then one region per group, `grp_bytes` apart from `off_grp`; the offsets
+// Xr ... misc lie within a group's region.
 struct StagedLayout {
-	int Pp, xcs, xvs, frs;
-	size_t off_T, off_Xr, off_Xq, off_Xc, off_VW, off_PK, off_HT, off_pt, off_pairs, off_F,
-	    off_G, off_fr, off_fidx, off_misc, bytes;
+	int Pp, xcs, xvs, frs, groups;
+	size_t off_T, off_HT, off_pt, off_pairs, off_grp, grp_bytes;
+	size_t off_Xr, off_Xq, off_Xc, off_VW, off_PK, off_F, off_G, off_fr, off_fidx, off_misc;
+	size_t bytes;
 };
 
-inline StagedLayout staged_layout(int n, int m, int P, int Pp)
+inline StagedLayout staged_layout(int n, int m, int P, int Pp, int groups = 1)
 {
 	StagedLayout L;
 	L.Pp = Pp;
 	L.xcs = n | 1;
 	L.xvs = n;
+	L.groups = groups;
 	auto a16 = [](size_t v) { return (v + 15) & ~size_t(15); };
 	size_t off = 0;
 	L.off_T = off;
 	off = a16(off + size_t(n) * Pp * 4);
+	L.off_HT = off;
+	off = a16(off + 64 * 4);
+	L.off_pt = off;
+	off = a16(off + size_t(m) * (n + 1) * 2);
+	L.off_pairs = off;
+	off = a16(off + size_t(P) * 4);
+	L.off_grp = off;
+	off = 0; // a group's region
 	L.off_Xr = off; // the cross-slice reduction reuses it after the backward pass
 	off = a16(off + std::max(size_t(n) * Pp * 2, size_t(kFamThreads) * 4));
 	L.off_Xq = off;
@@ -63,12 +80,6 @@ inline StagedLayout staged_layout(int n, int m, int P, int Pp)
 	off = a16(off + size_t(m) * L.xvs * 8);
 	L.off_PK = off;
 	off = a16(off + size_t(P) * 16);
-	L.off_HT = off;
-	off = a16(off + 64 * 4);
-	L.off_pt = off;
-	off = a16(off + size_t(m) * (n + 1) * 2);
-	L.off_pairs = off;
-	off = a16(off + size_t(P) * 4);
 	L.off_F = off;
 	off = a16(off + 32 * 4);
 	L.off_G = off;
@@ -80,8 +91,17 @@ inline StagedLayout staged_layout(int n, int m, int P, int Pp)
 	off = a16(off + size_t(n));
 	L.off_misc = off; // two 4-word job masks, then two claimed fathers
 	off += 32 + 16;
-	L.bytes = a16(off);
+	L.grp_bytes = a16(off);
+	L.bytes = L.off_grp + size_t(groups) * L.grp_bytes;
 	return L;
+}
+
+// Barrier of one group's NT threads (named barrier 1 + group; barrier 0
+// stays the CTA's).
+template <int NT>
+__device__ __forceinline__ void group_sync(int group)
+{
+	asm volatile("bar.sync %0, %1;" ::"r"(1 + group), "n"(NT) : "memory");
 }
 
 // Free positions of a walk mask in ascending order (words w[0..NW-1]).
@@ -203,8 +223,9 @@ constexpr int kSB = 4; // staged walks and sweep: entries loaded ahead per batch
 
 
 // Stages one instance's tables for staged_fathers: the packed Johnson
-// table, processing times, pairs, heads and tails. Every thread calls it; a
-// barrier must follow before staged_fathers reads them (its first one does).
+// table, processing times, pairs, heads and tails. Every thread of the CTA
+// calls it; a barrier of the whole CTA must follow before staged_fathers
+// reads them.
 __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
                                                    const uint32_t *__restrict__ tpack,
                                                    const StagedLayout &L, uint8_t *smem)
@@ -233,43 +254,54 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 	}
 }
 
-// One CTA bounds one father at a time; while its walkers run the backward
-// passes, warps 0-1 (idle then) claim the CTA's father after next and load
-// the next father's record into the other record buffer, so neither the
-// claim's round trip nor the record load sits between two fathers. Five
+// A group bounds one father at a time; while its walkers run the backward
+// passes, its warps 0-1 (idle then) claim the group's father after next and
+// load the next father's record into the other record buffer, so neither
+// the claim's round trip nor the record load sits between two fathers. Five
 // barriers per father: record ready, free-job columns, forward passes and
 // fronts, backward passes, children's bounds.
 //
 // staged_fathers bounds the fathers first, claim(first), claim(that), ...
 // until a claim returns nf or more, with the tables already staged
-// (staged_load_tables, followed by any barrier); every thread of a CTA of
-// NT threads (P <= NT - 64) calls it with the same arguments. Returns the
-// number of fathers it bounded.
+// (staged_load_tables, then a barrier of the CTA); every thread of group
+// `group` (NT threads from threadIdx.x = group * NT, P <= NT - 64) calls it
+// with the same arguments. Returns the number of fathers it bounded.
+//
+// The group's warps take their roles rotated by two warps per group (role
+// warp w is warp (w - 2 * group) mod NT/32 of the group), so that the
+// groups' front and back warps, which issue little, sit on different SM
+// sub-partitions (warp slot mod 4) and the walkers spread evenly over them.
 template <bool kWide, int NT, typename Claim>
 __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
                                     const uint8_t *__restrict__ jobposT, const StagedLayout &L,
-                                    uint8_t *smem, long long nf, long long first, Claim claim)
+                                    uint8_t *smem, int group, long long nf, long long first,
+                                    Claim claim)
 {
 	constexpr int NW = kWide ? 4 : 2; // 32-bit words of a job or position mask
+	constexpr int kWarps = NT / 32;
 	const int n = bp.n, m = bp.m, P = bp.P, Pp = L.Pp, xcs = L.xcs, xvs = L.xvs;
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int lane = int(threadIdx.x) & 31;
+	const int warp = ((int(threadIdx.x) >> 5) - group * kWarps + 2 * group) % kWarps; // role
+	const int tid = warp * 32 + lane;
+	uint8_t *gsm = smem + L.off_grp + size_t(group) * L.grp_bytes;
 	uint32_t *sT = reinterpret_cast<uint32_t *>(smem + L.off_T);
-	uint16_t *sXr = reinterpret_cast<uint16_t *>(smem + L.off_Xr);
-	uint32_t *sRed = reinterpret_cast<uint32_t *>(smem + L.off_Xr);
-	uint8_t *sXq = smem + L.off_Xq;
-	uint16_t *sXc = reinterpret_cast<uint16_t *>(smem + L.off_Xc);
-	uint16_t *sVW16 = reinterpret_cast<uint16_t *>(smem + L.off_VW);
-	const uint2 *sVW = reinterpret_cast<const uint2 *>(smem + L.off_VW);
-	uint4 *sPK = reinterpret_cast<uint4 *>(smem + L.off_PK);
+	uint16_t *sXr = reinterpret_cast<uint16_t *>(gsm + L.off_Xr);
+	uint32_t *sRed = reinterpret_cast<uint32_t *>(gsm + L.off_Xr);
+	uint8_t *sXq = gsm + L.off_Xq;
+	uint16_t *sXc = reinterpret_cast<uint16_t *>(gsm + L.off_Xc);
+	uint16_t *sVW16 = reinterpret_cast<uint16_t *>(gsm + L.off_VW);
+	const uint2 *sVW = reinterpret_cast<const uint2 *>(gsm + L.off_VW);
+	uint4 *sPK = reinterpret_cast<uint4 *>(gsm + L.off_PK);
 	int32_t *sHT = reinterpret_cast<int32_t *>(smem + L.off_HT); // heads[32], tails[32]
 	uint16_t *sPt = reinterpret_cast<uint16_t *>(smem + L.off_pt);
 	int32_t *sPairs = reinterpret_cast<int32_t *>(smem + L.off_pairs);
-	int32_t *sF = reinterpret_cast<int32_t *>(smem + L.off_F);
-	int32_t *sG = reinterpret_cast<int32_t *>(smem + L.off_G);
-	int16_t *sFrBuf = reinterpret_cast<int16_t *>(smem + L.off_fr); // [2][L.frs]
-	uint8_t *sFidx = smem + L.off_fidx;
-	uint32_t *sMaskBuf = reinterpret_cast<uint32_t *>(smem + L.off_misc); // [2][4]
-	long long *sNext = reinterpret_cast<long long *>(smem + L.off_misc + 32); // [2]
+	int32_t *sF = reinterpret_cast<int32_t *>(gsm + L.off_F);
+	int32_t *sG = reinterpret_cast<int32_t *>(gsm + L.off_G);
+	int16_t *sFrBuf = reinterpret_cast<int16_t *>(gsm + L.off_fr); // [2][L.frs]
+	uint8_t *sFidx = gsm + L.off_fidx;
+	uint32_t *sMaskBuf = reinterpret_cast<uint32_t *>(gsm + L.off_misc); // [2][4]
+	long long *sNext = reinterpret_cast<long long *>(gsm + L.off_misc + 32); // [2]
+	auto sync = [group]() { group_sync<NT>(group); };
 
 	// record of father g into buffer b; job ids clamped to [0, n): a
 	// malformed record gives wrong bounds, never an access outside the
@@ -293,7 +325,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 	const bool walker = t >= 0 && t < P;
 	int cur = 0;
 	for (long long f = first; f < nf;) {
-		__syncthreads(); // record f in buffer cur, its successor in sNext[cur]
+		sync(); // record f in buffer cur, its successor in sNext[cur]
 		const long long fn = sNext[cur];
 		const int16_t *sFr = sFrBuf + cur * L.frs;
 		uint32_t *sMask = sMaskBuf + 4 * cur;
@@ -324,7 +356,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		if (u == 2) {
 			// two leaves: makespans of front + (x, y) + back, both orders
 			staged_fronts(warp, lane, n, m, l1, l2, u, xvs, sPt, sFr, sF, sG, sVW16, true);
-			__syncthreads();
+			sync();
 			if (tid < 2) {
 				const int x = sFr[l1 + 1 + tid], y = sFr[l1 + 2 - tid];
 				int32_t v1 = 0, v2 = 0, mk = 0;
@@ -350,11 +382,11 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 			sFidx[j] = uint8_t(tid);
 			atomicOr(&sMask[j >> 5], 1u << (j & 31));
 		}
-		__syncthreads();
+		sync();
 		// a record whose free jobs repeat one another is skipped (its walks
 		// would find fewer than u positions)
 		if (__popc(sMask[0]) + __popc(sMask[1]) + __popc(sMask[2]) + __popc(sMask[3]) != u) {
-			__syncthreads(); // every thread has read the mask
+			sync(); // every thread has read the mask
 			if (tid < 4)
 				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
 			prefetch();
@@ -442,7 +474,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		} else if (tid < kFrontThreads) {
 			staged_fronts(warp, lane, n, m, l1, l2, u, xvs, sPt, sFr, sF, sG, sVW16);
 		}
-		__syncthreads(); // fronts, backs and every forward pass done
+		sync(); // fronts, backs and every forward pass done
 		if (walker) {
 			// the pair's constants for the children's bounds: the father's
 			// front on m1, m2 (the static heads without one) and back (0 on m1
@@ -495,7 +527,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
 			prefetch();
 		}
-		__syncthreads(); // every X_j and pair constant in place
+		sync(); // every X_j and pair constant in place
 		// the children's bounds: thread (column i, slice rs) of NS slices
 		// takes the pairs rs, rs + NS, ...; tid / u without an integer
 		// division ((tid + 1/2) / u lies at least 1/(2u) >= 1/256 from an
@@ -532,7 +564,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 			}
 		}
 		sRed[tid] = acc; // Xr is consumed
-		__syncthreads();
+		sync();
 		if (tid < u) {
 			uint32_t r = sRed[tid];
 			for (int k = 1; k < NS; ++k)

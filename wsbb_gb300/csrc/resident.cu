@@ -195,10 +195,10 @@ __device__ void bound_phase(const ResInst &I, unsigned long long ph, int own, ui
 		return; // uniform
 	auto claim = [&](long long) { return claim_father(I, ph, own); };
 	const long long done =
-	    I.wide ? staged::staged_fathers<true, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, nf,
-	                                                       first, claim)
-	           : staged::staged_fathers<false, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, nf,
-	                                                        first, claim);
+	    I.wide ? staged::staged_fathers<true, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, 0,
+	                                                       nf, first, claim)
+	           : staged::staged_fathers<false, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, 0,
+	                                                        nf, first, claim);
 	__threadfence(); // the CTA's child bounds, before they are counted
 	__syncthreads();
 	if (threadIdx.x == 0)
@@ -450,10 +450,10 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 		I.tpack = ctx->tables.tpack;
 		I.jobposT = ctx->tables.jobposT;
 		I.L = staged::staged_layout(ctx->bp.n, ctx->bp.m, ctx->bp.P, ctx->tables.Pp);
-		// the single-CTA phases' scratch: the per-father part of the window
-		// when it is large enough, else after the window
-		I.scratch_off = unsigned(I.L.off_HT - I.L.off_Xr) >= sizeof(ResScratch)
-		                    ? unsigned(I.L.off_Xr)
+		// the single-CTA phases' scratch: the per-father region (one group)
+		// when it is large enough, else after it
+		I.scratch_off = I.L.grp_bytes >= sizeof(ResScratch)
+		                    ? unsigned(I.L.off_grp)
 		                    : unsigned((I.L.bytes + 15) & ~size_t(15));
 		smem = std::max(smem, std::max(I.L.bytes, size_t(I.scratch_off) + sizeof(ResScratch)));
 		I.max_iters = cfgs[k].max_iters;
