@@ -152,6 +152,33 @@ __device__ __forceinline__ bool mask_has(const uint32_t (&w)[NW], int job)
 // child's back. Warp 0 the father's front F and the fronts, warp 1 its
 // reversed back G and the backs (each a wavefront, lane = machine, then one
 // lane per free job); with leaves_only, F and G alone.
+//
+// The wavefront's step s has lane k add job s - k's time on its machine to
+// max(its own time, lane k-1's); the times of kWaveBatch steps are loaded
+// before their steps run, so that only the steps' own chain (a shuffle, a
+// maximum and an add) is serial.
+constexpr int kWaveBatch = 8;
+template <typename TimeOf>
+__device__ __forceinline__ int32_t staged_wave(int lane, int m, int nj, TimeOf time_of)
+{
+	int32_t Fk = 0;
+	for (int s0 = 0; s0 < nj + m - 1; s0 += kWaveBatch) {
+		int32_t tv[kWaveBatch];
+#pragma unroll
+		for (int d = 0; d < kWaveBatch; ++d) {
+			const int i = s0 + d - lane;
+			tv[d] = (lane < m && i >= 0 && i < nj) ? int32_t(time_of(i)) : -1; // -1: no step
+		}
+#pragma unroll
+		for (int d = 0; d < kWaveBatch; ++d) {
+			const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
+			if (tv[d] >= 0)
+				Fk = max(Fk, lane > 0 ? left : 0) + tv[d];
+		}
+	}
+	return Fk;
+}
+
 __device__ __forceinline__ void staged_fronts(int warp, int lane, int n, int m, int l1, int l2,
                                               int u, int xvs, const uint16_t *pt,
                                               const int16_t *fr, int32_t *F, int32_t *G,
@@ -159,17 +186,8 @@ __device__ __forceinline__ void staged_fronts(int warp, int lane, int n, int m, 
 {
 	const int ld = n + 1;
 	if (warp == 0) {
-		int32_t Fk = 0;
-		const int nj = l1 + 1;
-		int32_t add = (lane < m && lane == 0 && nj > 0) ? pt[fr[0]] : 0;
-		for (int s = 0; s < nj + m - 1; ++s) {
-			const int i = s - lane, i1 = i + 1;
-			const int32_t next = (lane < m && i1 >= 0 && i1 < nj) ? pt[lane * ld + fr[i1]] : 0;
-			const int32_t left = __shfl_up_sync(0xffffffffu, Fk, 1);
-			if (lane < m && i >= 0 && i < nj)
-				Fk = max(Fk, lane > 0 ? left : 0) + add;
-			add = next;
-		}
+		const int32_t Fk =
+		    staged_wave(lane, m, l1 + 1, [&](int i) { return pt[lane * ld + fr[i]]; });
 		if (lane < m)
 			F[lane] = Fk;
 		if (leaves_only)
@@ -187,18 +205,9 @@ __device__ __forceinline__ void staged_fronts(int warp, int lane, int n, int m, 
 			}
 		}
 	} else if (warp == 1) {
-		int32_t Gq = 0;
-		const int nj = n - l2;
-		int32_t add = (lane < m && lane == 0 && nj > 0) ? pt[(m - 1) * ld + fr[n - 1]] : 0;
-		for (int s = 0; s < nj + m - 1; ++s) {
-			const int i = s - lane, i1 = i + 1;
-			const int32_t next =
-			    (lane < m && i1 >= 0 && i1 < nj) ? pt[(m - 1 - lane) * ld + fr[n - 1 - i1]] : 0;
-			const int32_t left = __shfl_up_sync(0xffffffffu, Gq, 1);
-			if (lane < m && i >= 0 && i < nj)
-				Gq = max(Gq, lane > 0 ? left : 0) + add;
-			add = next;
-		}
+		const int32_t Gq = staged_wave(lane, m, n - l2, [&](int i) {
+			return pt[(m - 1 - lane) * ld + fr[n - 1 - i]];
+		});
 		if (lane < m)
 			G[lane] = Gq;
 		if (leaves_only)
