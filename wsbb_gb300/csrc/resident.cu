@@ -9,6 +9,22 @@
 #include <string>
 #include <vector>
 
+// The search phases' bodies run on the first 256 threads of a CTA and
+// synchronise those alone, on barrier 4 (barrier 0 is the whole CTA's, 1
+// and 2 the family groups').
+#define WSBB_BODY_SYNC() asm volatile("bar.sync 4, 256;" ::: "memory")
+#define WSBB_BODY_SYNC_OR(p) wsbb_body_sync_or(p)
+__device__ __forceinline__ int wsbb_body_sync_or(int p)
+{
+	int r;
+	asm volatile("{\n\t.reg .pred a, b;\n\tsetp.ne.s32 a, %1, 0;\n\t"
+	             "bar.red.or.pred b, 4, 256, a;\n\tselp.s32 %0, 1, 0, b;\n\t}"
+	             : "=r"(r)
+	             : "r"(p)
+	             : "memory");
+	return r;
+}
+
 #include "family_staged.cuh"
 #include "search_host.h"
 
@@ -42,6 +58,7 @@ struct ResSync {
 	unsigned long long fam_done; // fathers bounded in the open phase
 	int stopped;                 // the search reached its iteration or node limit
 	int hold;                    // watchdog self-test: a flag nothing sets
+	int watchdog;                // a wait of this instance ran out
 };
 
 struct ResInst {
@@ -65,8 +82,15 @@ struct ResGlobal {
 	unsigned long long wait_ns;  // limit of every wait
 };
 
-constexpr int kResThreads = staged::kFamThreads;
+// CTAs of kResThreads: the phases' bodies on the first kResBodyThreads,
+// the family phase on kResGroups groups of staged::kFamThreads (as many as
+// the instance's shared memory allows), the element-wise phases on all.
+constexpr int kResBodyThreads = 256;
+constexpr int kResGroups = 2;
+constexpr int kResThreads = staged::kFamThreads * kResGroups;
 constexpr int kResCommitItems = 16;
+static_assert(kResBodyThreads == staged::kFamThreads && kResThreads == 2 * kResBodyThreads,
+              "the bodies' barrier (WSBB_BODY_SYNC) counts 256 threads");
 
 __device__ __forceinline__ unsigned long long gtimer()
 {
@@ -84,8 +108,8 @@ __device__ __forceinline__ T vload(const T *p)
 struct ResScratch {
 	CommitShared commit;
 	long long s_ll[32];
-	int tile[kScanItems * kResThreads + kScanItems * kResThreads / 32];
-	uint8_t inv[kResThreads / 32][WSBB_MAX_JOBS];
+	int tile[kScanItems * kResBodyThreads + kScanItems * kResBodyThreads / 32];
+	uint8_t inv[kResBodyThreads / 32][WSBB_MAX_JOBS];
 };
 
 // Group barrier; the last CTA to arrive runs act() (on its thread 0) before
@@ -116,7 +140,7 @@ __device__ bool group_barrier(const ResInst &I, ResGlobal *G, Act act)
 					break;
 				}
 				if (gtimer() - t0 > 2 * G->wait_ns) {
-					I.P.dev->error = WSBB_ERR_WATCHDOG;
+					atomicExch(&S->watchdog, 1);
 					atomicExch(&G->abort, 1);
 					ok = 0;
 					break;
@@ -145,7 +169,7 @@ __device__ int bounded_wait(const ResInst &I, ResGlobal *G, Cond cond)
 		if (vload(&G->abort))
 			return 0;
 		if (gtimer() - t0 > G->wait_ns) {
-			I.P.dev->error = WSBB_ERR_WATCHDOG;
+			atomicExch(&I.sync->watchdog, 1);
 			atomicExch(&G->abort, 1);
 			return 0;
 		}
@@ -182,26 +206,30 @@ __device__ long long claim_father(const ResInst &I, unsigned long long ph, int o
 }
 
 // Bounds fathers of instance I's open phase `ph` in this CTA (tables of I
-// staged), claiming from pool `own` first; adds them to the phase's count.
+// staged), each of the instance's I.L.groups groups on its own fathers,
+// claiming from pool `own` first; adds them to the phase's count. Every
+// thread of the CTA calls it.
 __device__ void bound_phase(const ResInst &I, unsigned long long ph, int own, uint8_t *smem)
 {
-	__shared__ long long s_first;
+	constexpr int NT = staged::kFamThreads;
+	__shared__ long long s_first[kResGroups];
 	const long long nf = (long long)(ph & kIdxMask);
-	if (threadIdx.x == 0)
-		s_first = claim_father(I, ph, own);
+	const int group = int(threadIdx.x) / NT;
+	if (threadIdx.x % NT == 0)
+		s_first[group] = group < I.L.groups ? claim_father(I, ph, own) : nf;
 	__syncthreads();
-	const long long first = s_first;
-	if (first >= nf)
-		return; // uniform
-	auto claim = [&](long long) { return claim_father(I, ph, own); };
-	const long long done =
-	    I.wide ? staged::staged_fathers<true, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, 0,
-	                                                       nf, first, claim)
-	           : staged::staged_fathers<false, kResThreads>(I.FA, I.bp, I.jobposT, I.L, smem, 0,
-	                                                        nf, first, claim);
-	__threadfence(); // the CTA's child bounds, before they are counted
+	const long long first = s_first[group];
+	long long done = 0;
+	if (first < nf) { // uniform in the group
+		auto claim = [&](long long) { return claim_father(I, ph, own); };
+		done = I.wide ? staged::staged_fathers<true, NT>(I.FA, I.bp, I.jobposT, I.L, smem, group,
+		                                                 nf, first, claim)
+		              : staged::staged_fathers<false, NT>(I.FA, I.bp, I.jobposT, I.L, smem, group,
+		                                                  nf, first, claim);
+	}
+	__threadfence(); // the group's child bounds, before they are counted
 	__syncthreads();
-	if (threadIdx.x == 0)
+	if (threadIdx.x % NT == 0 && done > 0)
 		atomicAdd(&I.sync->fam_done, (unsigned long long)done);
 }
 
@@ -213,6 +241,7 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 	ExDev *D = I.P.dev;
 	const bool leader = rank == 0;
 	const int nc = I.num_ctas, tid = threadIdx.x;
+	const bool body = tid < kResBodyThreads; // the threads that run the bodies
 	ResSync *S = I.sync;
 	staged::staged_load_tables(I.bp, I.tpack, I.L, smem);
 	// the watchdog self-test: the first barrier also waits for a flag that
@@ -230,7 +259,8 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 				S->stopped = 1;
 			__syncthreads();
 			if (!vload(&S->stopped)) {
-				commit_body<kResThreads, kResCommitItems>(I.P, X.commit, false);
+				if (body)
+					commit_body<kResBodyThreads, kResCommitItems>(I.P, X.commit, false);
 				__syncthreads();
 				if (tid < 32)
 					doom_body(I.P);
@@ -240,14 +270,16 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 			return;
 		if (vload(&D->done) || vload(&D->error) || vload(&S->stopped))
 			return;
-		select_count_body(I.P, rank, nc, X.s_ll);
+		if (body)
+			select_count_body(I.P, rank, nc, X.s_ll);
 		if (!group_barrier(I, G))
 			return;
-		if (leader)
-			select_plan_body<kResThreads>(I.P, X.s_ll);
+		if (leader && body)
+			select_plan_body<kResBodyThreads>(I.P, X.s_ll);
 		if (!group_barrier(I, G))
 			return;
-		select_write_body(I.P, rank, nc, X.s_ll);
+		if (body)
+			select_write_body(I.P, rank, nc, X.s_ll);
 		if (!group_barrier(I, G))
 			return;
 		make_children_body(I.P, 0, (long long)rank * kResThreads + tid,
@@ -288,11 +320,12 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 		            (long long)nc * (kResThreads / 32));
 		if (!group_barrier(I, G))
 			return;
-		if (leader)
-			kept_scan_body<kResThreads>(I.P, X.s_ll, X.tile);
+		if (leader && body)
+			kept_scan_body<kResBodyThreads>(I.P, X.s_ll, X.tile);
 		if (!group_barrier(I, G))
 			return;
-		emit_body(I.P, rank, nc, X.inv);
+		if (body)
+			emit_body(I.P, rank, nc, X.inv);
 		if (!group_barrier(I, G))
 			return;
 		if (leader && tid == 0)
@@ -422,6 +455,11 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 	const int wait_ms = opts && opts->wait_ms > 0 ? opts->wait_ms : 2000;
 	const int self_test = opts ? opts->self_test : 0;
 
+	int max_optin = 0;
+	e = cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+	if (e != cudaSuccess)
+		return ex_fail(c0, e, "device attribute");
+
 	// search states and layouts
 	std::vector<ResInst> H((size_t)count);
 	size_t smem = 0;
@@ -449,21 +487,23 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 		I.FA.stride = X->P.stride;
 		I.tpack = ctx->tables.tpack;
 		I.jobposT = ctx->tables.jobposT;
-		I.L = staged::staged_layout(ctx->bp.n, ctx->bp.m, ctx->bp.P, ctx->tables.Pp);
-		// the single-CTA phases' scratch: the per-father region (one group)
-		// when it is large enough, else after it
-		I.scratch_off = I.L.grp_bytes >= sizeof(ResScratch)
-		                    ? unsigned(I.L.off_grp)
-		                    : unsigned((I.L.bytes + 15) & ~size_t(15));
+		// the family groups: as many as fit one CTA's shared memory, with
+		// the single-CTA phases' scratch in the first group's region when
+		// it is large enough, else after the groups
+		for (int groups = kResGroups; groups >= 1; --groups) {
+			I.L = staged::staged_layout(ctx->bp.n, ctx->bp.m, ctx->bp.P, ctx->tables.Pp, groups);
+			I.scratch_off = I.L.grp_bytes >= sizeof(ResScratch)
+			                    ? unsigned(I.L.off_grp)
+			                    : unsigned((I.L.bytes + 15) & ~size_t(15));
+			if (std::max(I.L.bytes, size_t(I.scratch_off) + sizeof(ResScratch)) + 1024 <=
+			    size_t(max_optin))
+				break;
+		}
 		smem = std::max(smem, std::max(I.L.bytes, size_t(I.scratch_off) + sizeof(ResScratch)));
 		I.max_iters = cfgs[k].max_iters;
 		I.max_bounded = cfgs[k].max_bounded;
 		I.wide = ctx->bp.n > 64;
 	}
-	int max_optin = 0;
-	e = cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-	if (e != cudaSuccess)
-		return ex_fail(c0, e, "device attribute");
 	if (smem > size_t(max_optin))
 		return wsbb_set_error(c0, WSBB_ERR_ARG, "resident search: instances too large for one CTA");
 	e = allow_max_dynamic_smem(resident_kernel);
@@ -567,6 +607,8 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 		if (e != cudaSuccess)
 			break;
 		const int status = h.done ? 0 : 1;
+		if (hs[size_t(k)].watchdog && !h.error)
+			h.error = WSBB_ERR_WATCHDOG;
 		fill_stats(h, best_rec.data(), ctxs[k]->inst.n, status, ms * 1e-3, 1,
 		           ctxs[k]->bp.stride, &stats[k]);
 		if (h.error) {

@@ -14,6 +14,15 @@
 #include "node_features.cuh"
 #include "wsbb_internal.h"
 
+// The bodies below synchronise the threads that run them: the whole CTA,
+// unless the including unit runs them on part of its CTAs' threads and
+// defines both macros first (a barrier of those threads, and its
+// predicate-or form).
+#ifndef WSBB_BODY_SYNC
+#define WSBB_BODY_SYNC() __syncthreads()
+#define WSBB_BODY_SYNC_OR(p) __syncthreads_or(p)
+#endif
+
 namespace wsbb {
 
 // CONDEMNED: a marker the incumbent already prunes whose whole subtree is
@@ -149,7 +158,7 @@ __device__ T block_excl_scan(T v, Op op, T identity, T *scratch, T *total)
 	}
 	if (lane == 31)
 		scratch[warp] = x;
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	if (warp == 0) {
 		T w = lane < (NT / 32) ? scratch[lane] : identity;
 #pragma unroll
@@ -160,13 +169,13 @@ __device__ T block_excl_scan(T v, Op op, T identity, T *scratch, T *total)
 		}
 		scratch[lane] = w; // inclusive over warps
 	}
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	const T warp_prefix = warp == 0 ? identity : scratch[warp - 1];
 	const T excl_in_warp = __shfl_up_sync(0xffffffffu, x, 1);
 	const T excl = lane == 0 ? warp_prefix : op(warp_prefix, excl_in_warp);
 	if (total)
 		*total = scratch[NT / 32 - 1];
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	return excl;
 }
 
@@ -194,7 +203,7 @@ __device__ T block_excl_suffix_scan(T v, Op op, T identity, T *scratch)
 	}
 	if (lane == 0)
 		scratch[warp] = x; // inclusive suffix of the warp
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	if (warp == 0) {
 		T w = lane < NW ? scratch[lane] : identity;
 #pragma unroll
@@ -205,11 +214,11 @@ __device__ T block_excl_suffix_scan(T v, Op op, T identity, T *scratch)
 		}
 		scratch[lane] = w; // inclusive suffix over warps
 	}
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	const T warp_suffix = warp == NW - 1 ? identity : scratch[warp + 1];
 	const T excl_in_warp = __shfl_down_sync(0xffffffffu, x, 1);
 	const T excl = lane == 31 ? warp_suffix : op(warp_suffix, excl_in_warp);
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	return excl;
 }
 
@@ -243,7 +252,7 @@ __device__ long long cta_scan(long long count, Get get, Put put, long long *s_ll
 			const int j = k * NT + t;
 			tile[scan_pad(j)] = base + j < count ? get(base + j) : 0;
 		}
-		__syncthreads();
+		WSBB_BODY_SYNC();
 		int v[kScanItems];
 		int sum = 0;
 #pragma unroll
@@ -260,7 +269,7 @@ __device__ long long cta_scan(long long count, Get get, Put put, long long *s_ll
 			tile[scan_pad(t * kScanItems + k)] = run;
 			run += v[k];
 		}
-		__syncthreads();
+		WSBB_BODY_SYNC();
 #pragma unroll
 		for (int k = 0; k < kScanItems; ++k) {
 			const int j = k * NT + t;
@@ -268,7 +277,7 @@ __device__ long long cta_scan(long long count, Get get, Put put, long long *s_ll
 				put(base + j, carry + tile[scan_pad(j)]);
 		}
 		carry += tot;
-		__syncthreads(); // the tile is reused
+		WSBB_BODY_SYNC(); // the tile is reused
 	}
 	return carry;
 }
@@ -308,7 +317,7 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 		s_pend[i] = D->pend[i];
 		s_sfx[i] = 0;
 	}
-	__syncthreads();
+	WSBB_BODY_SYNC();
 
 	long long top = D->top;
 	const int ub0 = D->ub;
@@ -329,7 +338,7 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 		}
 		// leaves are rare: without one in the chunk the incumbent cannot
 		// change in it, and both leaf scans below are skipped
-		const int any_leaf = __syncthreads_or(leaf_min != INT_MAX);
+		const int any_leaf = WSBB_BODY_SYNC_OR(leaf_min != INT_MAX);
 		const int ub_in =
 		    any_leaf ? min(ub, block_excl_scan<NT>(leaf_min, MinOp(), INT_MAX, s_int,
 		                                                    (int *)nullptr))
@@ -427,7 +436,7 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 					has_np |= e[i].state == ST_BRANCHED && e[i].npruned;
 				}
 			}
-			if (__syncthreads_or(has_np)) {
+			if (WSBB_BODY_SYNC_OR(has_np)) {
 				int later = block_excl_suffix_scan<NT>(loc_min, MinOp(), INT_MAX, s_int);
 				if (t == 0)
 					s_dmin = min(later, loc_min);
@@ -441,12 +450,12 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 						later = e[i].depth;
 					}
 				}
-				__syncthreads();
+				WSBB_BODY_SYNC();
 			} else {
 				const int dm = block_reduce<NT>(loc_min, MinOp(), INT_MAX, s_int);
 				if (t == 0)
 					s_dmin = dm;
-				__syncthreads();
+				WSBB_BODY_SYNC();
 			}
 			const int dmin = s_dmin;
 			for (int d = t; d <= n; d += NT) {
@@ -504,7 +513,7 @@ __device__ void commit_body(const ExParams &P, CommitShared &sh, bool reset_clai
 		if ((t & 31) == 0)
 			atomicAdd(&s_cnt[q], cv[q]);
 	}
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	if (t == 0) {
 		D->branched += s_cnt[0];
 		D->pruned += s_cnt[1];
@@ -1263,7 +1272,7 @@ __global__ void __launch_bounds__(kPartialThreads) partial_kernel(ExParams P, Bo
 		for (uint32_t i = threadIdx.x; i < bp.t8.bytes / 16; i += blockDim.x)
 			dst[i] = src[i];
 	}
-	__syncthreads();
+	WSBB_BODY_SYNC();
 	const int n = P.n, m = bp.m, K = P.K;
 	const uint2 *tj = reinterpret_cast<const uint2 *>(smem);
 	const int32_t *pt = reinterpret_cast<const int32_t *>(smem + bp.t8.off_pt);
