@@ -317,9 +317,21 @@ def lb2_pool_section(dev, stream, sptr, peak, launches: int) -> dict:
 def proof_section() -> dict:
     from wsbb_gb300 import search_bench
     out = search_bench.run(PROOF_N, PROOF_M, PROOF_SEEDS, verbose=False, tune=True)
+    import wsbb_gb300 as W
+    from wsbb_gb300.explorer import explore
+    res_s, res_ok = 0.0, True
+    for sd in PROOF_SEEDS:
+        p = W.gen_instance(sd, PROOF_N, PROOF_M)
+        ctx = W.Context(p)
+        r = explore(ctx, ub0=W.neh(p)[0], best=99999, window=out["shape"]["window"],
+                    resident=True)
+        res_s += r["seconds"]
+        res_ok = res_ok and r["status"] == 0
+        ctx.close()
     return {"workload": f"exact DFS to a proven optimum, n={PROOF_N} m={PROOF_M}, seeds "
                         f"{list(PROOF_SEEDS)}, NEH incumbent, best=99999 (the reference "
                         "default), autotuned window and tile",
+            "resident_time_to_proof_s": res_s, "resident_all_proved": res_ok,
             "shape": out["shape"],
             "all_proved": out["all_proved"], "time_to_proof_s": out["seconds"],
             "bounded_nodes": out["bounded"], "bounded_nodes_per_s": out["bounded_per_s"],
@@ -452,6 +464,10 @@ def run_gpu(args) -> None:
                       stream=sptr, child_lb2=True,
                       window=win)
         arms = {"per_child_lb2": arm(per, per["seconds"]), "family_lb2": arm(fam, per["seconds"])}
+        # the resident search stopped at the step's iteration count: the same prefix
+        res = explore(ctx, ub0=ub0, best=ub0, max_iters=fam["iterations"], stream=sptr,
+                      window=win, resident=True)
+        arms["resident_family_lb2"] = arm(res, per["seconds"])
         if os.path.exists(MODEL):
             model = Model(S_N, S_M)
             model.load(MODEL)

@@ -8,9 +8,16 @@ bounded nodes: 10^9, the cap the workload sets for its n = 100 instances,
 applied to every instance so that the ones that cannot be proved in
 minutes end too). `resident` is the whole set in one launch of resident
 CTAs (wsbb_explore_resident: a group of CTAs per instance, fathers stolen
-between CTAs and from the instances still running). The arms below are
-then compared at a smaller budget (`cmp_budget`), each over the same
-instances and trees, checked equal.
+between CTAs and from the instances still running). Against it stands the
+single-instance rate of each shape: the shape's instance with the most
+nodes in the launch, alone, the graph-launched search to its proof or
+`single_budget` nodes (a small proof's rate says little of a long search's), at window
+16384 (the headline's) or, where its stack would overflow, 4096; the time the
+set would take run one instance after another at those rates
+(`sequential_estimate_s`: each shape's nodes in the resident launch over
+its single-instance rate) over the launch's time is `vs_sequential`. The
+arms below are then compared at a smaller budget (`cmp_budget`), each over
+the same instances and trees, checked equal.
 
 Instance i (seed i) has n = (20, 50, 100)[i % 3] jobs and m = (5, 10,
 20)[(i // 3) % 3] machines, times uniform in [1, 99] and the NEH incumbent;
@@ -60,8 +67,9 @@ def capacity_of(n: int) -> int:
 
 def run(instances: int = 64, threads: int = 8, budget: int = 10**9, cmp_budget: int = 2 * 10**7,
         window: int = 2048, K: int = 16, device: int = 0, arms=ARMS, best_mode: str = "ub0",
-        full: bool = True) -> dict:
+        full: bool = True, single_budget: int = 2 * 10**8) -> dict:
     from .bound import Context, gen_instance, neh
+    from ._lib import WsbbError
     from .explorer import explore, explore_resident
     from .learned import Model, explore_learned
 
@@ -108,6 +116,32 @@ def run(instances: int = 64, threads: int = 8, budget: int = 10**9, cmp_budget: 
             d["instances"] += 1
             d["bounded"] += r["bounded"]
             d["proved"] += int(r["status"] == 0)
+        # single-instance rates: each shape's heaviest instance alone
+        est = 0.0
+        heaviest: dict[str, dict] = {}
+        for it in items:
+            key = f"n{it['n']}_m{it['m']}"
+            if key not in heaviest or rs[it["seed"]]["bounded"] > rs[heaviest[key]["seed"]]["bounded"]:
+                heaviest[key] = it
+        for key, it in heaviest.items():
+            d = out["per_shape"][key]
+            for w in (16384, 4096):
+                try:
+                    kw = dict(ub0=it["ub0"], best=it["best"], window=w,
+                              capacity=2 * capacity_of(it["n"]))
+                    explore(it["ctx"], max_bounded=min(budget, 10**6), **kw)
+                    r = explore(it["ctx"], max_bounded=min(budget, single_budget), **kw)
+                    break
+                except WsbbError as e:
+                    if e.code != -6 or w == 4096:
+                        raise
+            d["single"] = {"seed": it["seed"], "window": w, "bounded": r["bounded"],
+                           "seconds": r["seconds"],
+                           "bounded_per_s": r["bounded"] / r["seconds"],
+                           "proved": r["status"] == 0}
+            est += d["bounded"] / d["single"]["bounded_per_s"]
+        out["resident_full"]["sequential_estimate_s"] = est
+        out["resident_full"]["vs_sequential"] = est / wall
 
     # the arms at the comparison budget
     results: dict[str, dict[int, dict]] = {a: {} for a in arms}
