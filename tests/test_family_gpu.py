@@ -126,6 +126,57 @@ def test_family_bounds_equal_per_child_kernel(env):
     assert torch.equal(lb, ref)
 
 
+@pytest.mark.parametrize("n,m", [(50, 20), (50, 5), (100, 20)])
+def test_family_skips_malformed_fathers(env, oracle, n, m):
+    """Fathers the kernel must pass over, between valid ones in one batch
+    (so that a group meets them amid its other fathers): a repeated free
+    job, a child range of the wrong size, cursors out of range. The valid
+    fathers' bounds equal the oracle's; the others' children stay as they
+    were."""
+    torch, W = env
+    rng = np.random.default_rng(n + m)
+    p = W.gen_instance(5, n, m)
+    ctx = W.Context(p)
+    count = 2400 if n <= 50 else 600
+    perms, l1, l2 = random_fathers(rng, n, count)
+    fathers = W.pack_records(perms, l1, l2)
+    kinds = np.zeros(count, dtype=np.int32)            # 0 valid
+    kinds[5::7] = 1                                    # a repeated free job
+    kinds[3::11] = 2                                   # a child range of the wrong size
+    kinds[8::13] = 3                                   # l1 below -1
+    sizes = []
+    for i in range(count):
+        u = int(l2[i] - l1[i] - 1)
+        k = 2 if u == 2 else 2 * u
+        if kinds[i] == 1:
+            if u < 3:
+                kinds[i] = 0
+            else:
+                fathers[i, l1[i] + 2] = fathers[i, l1[i] + 1]
+        elif kinds[i] == 2:
+            k += 2
+        elif kinds[i] == 3:
+            fathers[i, n] = -3
+        sizes.append(k)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    d_f = torch.from_numpy(fathers).cuda()
+    d_off = torch.from_numpy(off).cuda()
+    lb = torch.full((int(off[-1]),), -7, dtype=torch.int32, device="cuda")
+    job = torch.full((int(off[-1]),), -7, dtype=torch.int16, device="cuda")
+    ctx.decompose_lb2(d_f.data_ptr(), count, d_off.data_ptr(), lb.data_ptr(), job.data_ptr())
+    torch.cuda.synchronize()
+    lb, job = lb.cpu().numpy(), job.cpu().numpy()
+    valid = np.flatnonzero(kinds == 0)
+    assert len(valid) > count // 2 and (kinds == 1).sum() > count // 20
+    kids, koff = W.expand_children(fathers[valid], n)
+    kp, k1, k2 = W.unpack_records(kids, n)
+    want = oracle.Bound(p).eval_batch(kp, k1, k2)
+    got = np.concatenate([lb[off[f]:off[f + 1]] for f in valid])
+    np.testing.assert_array_equal(got, want)
+    for f in np.flatnonzero(kinds != 0):
+        assert (lb[off[f]:off[f + 1]] == -7).all() and (job[off[f]:off[f + 1]] == -7).all(), f
+
+
 @pytest.mark.parametrize("n,m,seed,best", [(20, 20, 1, "ub0"), (50, 10, 0, "default"),
                                            (12, 5, 3, "default")])
 def test_search_same_tree_family_and_per_child(env, n, m, seed, best):

@@ -34,20 +34,21 @@ constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 //    the position q in rows [k][Pp] (lanes walk in step, so these accesses
 //    are conflict-free too) and the backward pass reads them back instead
 //    of walking the position masks a second time;
-//  * the backward pass leaves X_j per pair and free position (its column,
-//    not the job), and the children's bounds are formed afterwards by every
-//    thread of the CTA, lanes on consecutive columns of one pair: the
-//    fronts and backs they read (per machine and column) and the X_j are
-//    consecutive words, and both children's three terms are computed as
-//    16-bit halves of one word (add, then one three-way and one two-way
-//    unsigned 16-bit maximum).
+//  * the backward pass leaves X_j per pair and job, and the children's
+//    bounds are formed afterwards by every thread of the group, lanes on
+//    consecutive columns (free positions) of one pair: the fronts and backs
+//    they read (per machine and column) are consecutive words, the X_j one
+//    pair's row (at n <= 64 at most 32 consecutive words: distinct banks),
+//    and both children's three terms are computed as 16-bit halves of one
+//    word (add, then one three-way and one two-way unsigned 16-bit
+//    maximum).
 // The CTA's tables first (T, heads and tails, processing times, pairs),
 // then one region per group, `grp_bytes` apart from `off_grp`; the offsets
 // Xr ... misc lie within a group's region.
 struct StagedLayout {
 	int Pp, xcs, xvs, frs, groups;
 	size_t off_T, off_HT, off_pt, off_pairs, off_grp, grp_bytes;
-	size_t off_Xr, off_Xq, off_Xc, off_VW, off_PK, off_F, off_G, off_fr, off_fidx, off_misc;
+	size_t off_Xr, off_Xq, off_Xc, off_VW, off_PK, off_F, off_G, off_fr, off_misc;
 	size_t bytes;
 };
 
@@ -87,8 +88,6 @@ inline StagedLayout staged_layout(int n, int m, int P, int Pp, int groups = 1)
 	L.frs = (n + 4 + 7) & ~7; // two record buffers
 	L.off_fr = off;
 	off = a16(off + size_t(2 * L.frs) * 2);
-	L.off_fidx = off;
-	off = a16(off + size_t(n));
 	L.off_misc = off; // two 4-word job masks, then two claimed fathers
 	off += 32 + 16;
 	L.grp_bytes = a16(off);
@@ -265,10 +264,10 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 
 // A group bounds one father at a time; while its walkers run the backward
 // passes, its warps 0-1 (idle then) claim the group's father after next and
-// load the next father's record into the other record buffer, so neither
-// the claim's round trip nor the record load sits between two fathers. Five
-// barriers per father: record ready, free-job columns, forward passes and
-// fronts, backward passes, children's bounds.
+// load the next father's record and job mask into the other buffers, so
+// neither the claim's round trip nor the record load sits between two
+// fathers. Four barriers per father: record and mask ready, forward passes
+// and fronts, backward passes, children's bounds.
 //
 // staged_fathers bounds the fathers first, claim(first), claim(that), ...
 // until a claim returns nf or more, with the tables already staged
@@ -307,40 +306,50 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 	int32_t *sF = reinterpret_cast<int32_t *>(gsm + L.off_F);
 	int32_t *sG = reinterpret_cast<int32_t *>(gsm + L.off_G);
 	int16_t *sFrBuf = reinterpret_cast<int16_t *>(gsm + L.off_fr); // [2][L.frs]
-	uint8_t *sFidx = gsm + L.off_fidx;
 	uint32_t *sMaskBuf = reinterpret_cast<uint32_t *>(gsm + L.off_misc); // [2][4]
 	long long *sNext = reinterpret_cast<long long *>(gsm + L.off_misc + 32); // [2]
 	auto sync = [group]() { group_sync<NT>(group); };
 
-	// record of father g into buffer b; job ids clamped to [0, n): a
-	// malformed record gives wrong bounds, never an access outside the
-	// tables. Threads t0 .. t0 + nt - 1.
+	// record of father g into buffer b, and its free jobs into job mask b
+	// (zeroed before); job ids clamped to [0, n): a malformed record gives
+	// wrong bounds, never an access outside the tables. Threads t0 .. t0 +
+	// nt - 1.
 	auto load_record = [&](long long g, int b, int t0, int nt) {
 		if (g >= nf)
 			return;
 		const long long ri = A.ridx ? A.ridx[g] : g;
 		const int16_t *g_fr = reinterpret_cast<const int16_t *>(A.fathers + ri * A.stride);
 		int16_t *dst = sFrBuf + b * L.frs;
-		for (int i = tid - t0; i < n + 2; i += nt)
-			dst[i] = i < n ? int16_t(min(max(int(g_fr[i]), 0), n - 1)) : g_fr[i];
+		const int gl1 = g_fr[n], gl2 = g_fr[n + 1];
+		for (int i = tid - t0; i < n + 2; i += nt) {
+			const int v = i < n ? min(max(int(g_fr[i]), 0), n - 1) : int(g_fr[i]);
+			dst[i] = int16_t(v);
+			if (i > gl1 && i < gl2 && i < n)
+				atomicOr(&sMaskBuf[4 * b + (v >> 5)], 1u << (v & 31));
+		}
 	};
 	if (tid < 8)
 		sMaskBuf[tid] = 0;
 	if (tid == 0)
 		sNext[0] = first < nf ? claim(first) : nf;
+	sync(); // the masks are clear
 	load_record(first, 0, 0, NT);
 	long long done = 0;
 	const int t = tid - kFrontThreads; // walker: pair t
 	const bool walker = t >= 0 && t < P;
 	int cur = 0;
 	for (long long f = first; f < nf;) {
-		sync(); // record f in buffer cur, its successor in sNext[cur]
+		sync(); // record f and its job mask in buffer cur, its successor in sNext[cur]
 		const long long fn = sNext[cur];
 		const int16_t *sFr = sFrBuf + cur * L.frs;
 		uint32_t *sMask = sMaskBuf + 4 * cur;
 		const int l1 = sFr[n], l2 = sFr[n + 1];
 		const int u = l2 - l1 - 1;
 		const long long c0 = A.child_off[f];
+		// the other mask buffer (its father is done) is cleared for the
+		// next record, which prefetch() loads after a barrier at least
+		if (tid < 4)
+			sMaskBuf[4 * (cur ^ 1) + tid] = 0;
 		// the next record and the claim after it, by warps 0-1 while they
 		// have nothing else to do
 		auto prefetch = [&]() {
@@ -352,10 +361,8 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		};
 		// cursors outside -1 <= l1, l2 <= n with two free jobs or more, or a
 		// child range of another size: the father is skipped
-		// (every path clears the other job mask, its father's being done)
 		if (l1 < -1 || l2 > n || u < 2 || A.child_off[f + 1] - c0 != (u == 2 ? 2 : 2 * u)) {
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
+			sync(); // the other mask is clear
 			prefetch();
 			++done;
 			f = fn;
@@ -377,27 +384,16 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 				A.child_lb[c0 + tid] = mk;
 				A.child_job[c0 + tid] = int16_t(x);
 			}
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
 			prefetch();
 			++done;
 			f = fn;
 			cur ^= 1;
 			continue;
 		}
-		// free jobs: their columns and the job mask
-		if (tid < u) {
-			const int j = sFr[l1 + 1 + tid];
-			sFidx[j] = uint8_t(tid);
-			atomicOr(&sMask[j >> 5], 1u << (j & 31));
-		}
-		sync();
 		// a record whose free jobs repeat one another is skipped (its walks
 		// would find fewer than u positions)
 		if (__popc(sMask[0]) + __popc(sMask[1]) + __popc(sMask[2]) + __popc(sMask[3]) != u) {
-			sync(); // every thread has read the mask
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
+			sync(); // the other mask is clear
 			prefetch();
 			++done;
 			f = fn;
@@ -495,7 +491,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 			sPK[t] = make_uint4(uint32_t(Bsum + r2) | uint32_t(Bsum + f2) << 16,
 			                    uint32_t(r2) | uint32_t(f1) << 16,
 			                    uint32_t(Asum + r1) | uint32_t(Asum + f1) << 16,
-			                    uint32_t(ma * xvs) | uint32_t(mb * xvs) << 16);
+			                    uint32_t(ma * xvs * 8) | uint32_t(mb * xvs * 8) << 16);
 			// backward: X_j = max(Csuf + Apre, Bsuf + Cpre) at each free job
 			int32_t cs = kNeg, bs = 0, R = Asum; // R = A minus the suffix's a
 			auto step = [&](uint32_t e, int32_t pre, int col) {
@@ -522,7 +518,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 						e[j] = sT[q[j] * Pp + t];
 #pragma unroll
 					for (int j = 0; j < kSB; ++j)
-						col[j] = sFidx[e[j] & 127u];
+						col[j] = int(e[j] & 127u);
 #pragma unroll
 					for (int j = 0; j < kSB; ++j)
 						if (k0 - j >= 0)
@@ -530,10 +526,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 				}
 			}
 		} else {
-			// warps 0-1: clear the other mask buffer (its father is done),
-			// then claim and load ahead
-			if (tid < 4)
-				sMaskBuf[4 * (cur ^ 1) + tid] = 0;
+			// warps 0-1: claim and load ahead
 			prefetch();
 		}
 		sync(); // every X_j and pair constant in place
@@ -546,6 +539,8 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		uint32_t acc = 0; // (BEGIN bound | END bound << 16)
 		if (rs < NS) {
 			const int i = tid - rs * u;
+			const int ji = sFr[l1 + 1 + i]; // the column's job: its X_j entry
+			const uint8_t *vwi = reinterpret_cast<const uint8_t *>(sVW + i);
 			for (int p0 = rs; p0 < P; p0 += kSB * NS) {
 				uint4 pk[kSB];
 				uint32_t x[kSB];
@@ -554,12 +549,12 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 				for (int j = 0; j < kSB; ++j) {
 					const int p = min(p0 + j * NS, P - 1);
 					pk[j] = sPK[p];
-					x[j] = sXc[p * xcs + i];
+					x[j] = sXc[p * xcs + ji];
 				}
 #pragma unroll
 				for (int j = 0; j < kSB; ++j) {
-					e1[j] = sVW[(pk[j].w & 0xffffu) + i];
-					e2[j] = sVW[(pk[j].w >> 16) + i];
+					e1[j] = *reinterpret_cast<const uint2 *>(vwi + (pk[j].w & 0xffffu));
+					e2[j] = *reinterpret_cast<const uint2 *>(vwi + (pk[j].w >> 16));
 				}
 				// a repeated last pair (past P) only repeats a maximum
 #pragma unroll
