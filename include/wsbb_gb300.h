@@ -235,16 +235,21 @@ int wsbb_explore(wsbb_ctx *ctx, const wsbb_explore_cfg *cfg, wsbb_stats *stats,
  * (window, capacity, best, ub0, max_iters, max_bounded apply per instance;
  * no WSBB_EXPLORE_RESUME, no WSBB_EXPLORE_CHILD_LB2). Instances must be on
  * one device, fit the staged family bounds (times <= 127, m <= 20) and
- * number at most the resident CTAs (twice the SM count for n = 50, m = 20).
- * Every wait between CTAs gives up after opts->wait_ms (0: 2000 ms): the
- * launch then ends with WSBB_ERR_WATCHDOG and the contexts stay usable.
- * opts->self_test = 1 makes the first wait also wait for a flag that
- * nothing sets, so that the watchdog must run out (a test of that path).
- * opts may be NULL. stats[k]: instance k; `seconds` is the launch's time.
+ * number at most the resident CTAs (the SM count). Each instance's
+ * iterations run on a group of CTAs, an equal share of the grid (at most
+ * opts->group_ctas when it is above 0); the CTAs left over, and those of
+ * instances that have ended, take fathers from the bound phases of the
+ * instances still running. Every wait between CTAs gives up after opts->wait_ms (0:
+ * 2000 ms): the launch then ends with WSBB_ERR_WATCHDOG and the contexts
+ * stay usable. opts->self_test = 1 makes the first wait also wait for a
+ * flag that nothing sets, so that the watchdog must run out (a test of that
+ * path). opts may be NULL. stats[k]: instance k; `seconds` is the launch's
+ * time.
  */
 typedef struct {
 	int32_t wait_ms;
 	int32_t self_test;
+	int32_t group_ctas;
 } wsbb_resident_opts;
 #define WSBB_EXPLORE_RESIDENT 8 /* wsbb_explore: run as the resident search */
 int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count, const wsbb_explore_cfg *cfgs,

@@ -89,6 +89,35 @@ def test_resident_many_instances_one_launch(W):
     assert 0 < finished < len(shapes)
 
 
+def test_resident_small_groups_and_free_thieves(W):
+    """Groups capped below an equal share (group_ctas): the CTAs outside
+    every group only take fathers from the bound phases, and the trees stay
+    the graph-launched search's."""
+    Wm, E = W
+    p = Wm.gen_instance(9, 50, 10)
+    neh, _ = Wm.neh(p)
+    ctx = Wm.Context(p)
+    want = E.explore(ctx, ub0=neh, best=neh, window=1024)
+    rc, got = E.explore_resident([ctx], ub0s=[neh], bests=[neh], window=1024, group_ctas=4)
+    assert rc == 0 and got[0]["status"] == 0
+    same(got[0], want, "one instance, groups of 4")
+    shapes = [(16, 10, 2), (20, 5, 7), (50, 5, 32), (50, 20, 0), (100, 10, 2)]
+    ctxs, ubs, wants = [], [], []
+    for n, m, sd in shapes:
+        q = Wm.gen_instance(sd, n, m)
+        ub, _ = Wm.neh(q)
+        c = Wm.Context(q)
+        ctxs.append(c)
+        ubs.append(ub)
+        wants.append(E.explore(c, ub0=ub, best=ub, window=512, graph_iters=1, max_iters=200))
+    rc, got = E.explore_resident(ctxs, ub0s=ubs, bests=ubs, window=512, max_iters=200,
+                                 group_ctas=2)
+    assert rc == 0
+    for (n, m, sd), g, w in zip(shapes, got, wants):
+        assert g["status"] == w["status"], (n, m, sd)
+        same(g, w, f"n{n} m{m} s{sd}, groups of 2")
+
+
 def test_resident_watchdog_ends_the_launch(W):
     """A wait that nothing ends (the self-test flag) runs out after its
     limit: the launch ends with WSBB_ERR_WATCHDOG, and the contexts run a

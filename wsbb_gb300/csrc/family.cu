@@ -715,8 +715,11 @@ __global__ void __launch_bounds__(staged::kMaxCtaThreads, 1)
 	staged::staged_fathers<kWide, NT>(A, bp, jobposT, L, smem, group, nf,
 	                                  (long long)group * gridDim.x + blockIdx.x,
 	                                  [&](long long after) -> long long {
-		                                  return A.next ? base + (long long)atomicAdd(A.next, 1ull)
-		                                                : after + base;
+		                                  // one warp calls it: lane 0 claims for all
+		                                  long long c = after + base;
+		                                  if (A.next && (threadIdx.x & 31) == 0)
+			                                  c = base + (long long)atomicAdd(A.next, 1ull);
+		                                  return __shfl_sync(0xffffffffu, c, 0);
 	                                  });
 }
 

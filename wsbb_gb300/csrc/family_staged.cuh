@@ -273,7 +273,9 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 // until a claim returns nf or more, with the tables already staged
 // (staged_load_tables, then a barrier of the CTA); every thread of group
 // `group` (NT threads from threadIdx.x = group * NT, P <= NT - 64) calls it
-// with the same arguments. Returns the number of fathers it bounded.
+// with the same arguments. Every lane of one warp calls claim(after) with
+// the same argument, and it returns the same index on every lane. Returns
+// the number of fathers it bounded.
 //
 // The group's warps take their roles rotated by two warps per group (role
 // warp w is warp (w - 2 * group) mod NT/32 of the group), so that the
@@ -330,8 +332,11 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 	};
 	if (tid < 8)
 		sMaskBuf[tid] = 0;
-	if (tid == 0)
-		sNext[0] = first < nf ? claim(first) : nf;
+	if (warp == 0) {
+		const long long c = first < nf ? claim(first) : nf;
+		if (lane == 0)
+			sNext[0] = c;
+	}
 	sync(); // the masks are clear
 	load_record(first, 0, 0, NT);
 	long long done = 0;
@@ -354,8 +359,11 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		// have nothing else to do
 		auto prefetch = [&]() {
 			if (tid < kFrontThreads) {
-				if (tid == 0)
-					sNext[cur ^ 1] = fn < nf ? claim(fn) : nf;
+				if (warp == 0) {
+					const long long c = fn < nf ? claim(fn) : nf;
+					if (lane == 0)
+						sNext[cur ^ 1] = c;
+				}
 				load_record(fn, cur ^ 1, 0, kFrontThreads);
 			}
 		};

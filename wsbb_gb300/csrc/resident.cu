@@ -46,15 +46,25 @@ namespace {
 // by a %globaltimer limit; one that runs out sets WSBB_ERR_WATCHDOG on its
 // instance and aborts the launch, every CTA leaving at its next wait.
 
-// Father pools: claim counter = phase tag << kTagShift | next index. A
-// claim is valid only for the tag it was made under and below its pool's
-// end, so a late claim can never take a father of another iteration.
+// Father pools: a phase's fathers are split into pools of about
+// kFathersPerPool (at most kMaxPools, one per lane of a warp), each with a
+// claim counter = phase tag << kTagShift | next index. A claim is valid
+// only for the tag it was made under and below its pool's end, so a late
+// claim can never take a father of another iteration. The open phase's
+// word holds tag << kTagShift | pools << kPoolShift | fathers, so every
+// claimer splits the fathers into the same pools. A claim is made by one
+// warp, which reads every pool's counter at once and takes the first
+// non-empty pool from its own on.
 constexpr int kTagShift = 40;
 constexpr unsigned long long kIdxMask = (1ull << kTagShift) - 1;
+constexpr int kPoolShift = 32;
+constexpr unsigned long long kNfMask = (1ull << kPoolShift) - 1;
+constexpr int kMaxPools = 32;
+constexpr int kFathersPerPool = 16;
 
 struct ResSync {
 	unsigned arrive, gen;        // group barrier
-	unsigned long long phase;    // open family phase: tag << kTagShift | fathers (0: closed)
+	unsigned long long phase;    // open family phase (see kPoolShift; 0: closed)
 	unsigned long long fam_done; // fathers bounded in the open phase
 	int stopped;                 // the search reached its iteration or node limit
 	int hold;                    // watchdog self-test: a flag nothing sets
@@ -70,7 +80,7 @@ struct ResInst {
 	staged::StagedLayout L;
 	unsigned scratch_off;        // single-CTA phases' shared memory
 	ResSync *sync;
-	unsigned long long *heads;   // [num_ctas] pool claim counters
+	unsigned long long *heads;   // [kMaxPools] pool claim counters
 	long long max_iters, max_bounded;
 	int first_cta, num_ctas, wide;
 };
@@ -183,26 +193,37 @@ __device__ __forceinline__ long long pool_start(long long nf, int v, int nc)
 	return nf * v / nc;
 }
 
-// A claim in instance I's open phase `ph` (tag << kTagShift | fathers),
-// first from pool `own` then from the others; nf when all are empty. By
-// compare-and-swap, so it only ever takes an index of that phase.
+// A claim in instance I's open phase `ph` by every lane of one warp: lane
+// k looks at pool (own + k) mod pools, and the first lane whose pool still
+// holds fathers of that phase takes one by compare-and-swap (so only an
+// index of that phase is ever taken); nf on every lane when every pool is
+// empty. A failed swap means another claim succeeded, so the loop ends.
 __device__ long long claim_father(const ResInst &I, unsigned long long ph, int own)
 {
-	const long long nf = (long long)(ph & kIdxMask);
+	const int lane = int(threadIdx.x) & 31;
+	const long long nf = (long long)(ph & kNfMask);
+	const int np = int((ph & kIdxMask) >> kPoolShift);
 	const unsigned long long tag = ph >> kTagShift;
-	const int nc = I.num_ctas;
-	for (int k = 0; k < nc; ++k) {
-		const int v = (own + k) % nc;
-		const long long end = pool_start(nf, v + 1, nc);
-		unsigned long long h = vload(&I.heads[v]);
-		while ((h >> kTagShift) == tag && (long long)(h & kIdxMask) < end) {
-			const unsigned long long seen = atomicCAS(&I.heads[v], h, h + 1);
-			if (seen == h)
-				return (long long)(h & kIdxMask);
-			h = seen;
+	const int v = (own + lane) % max(np, 1);
+	const long long end = pool_start(nf, v + 1, max(np, 1));
+	for (;;) {
+		unsigned long long h = 0;
+		bool live = false;
+		if (lane < np) {
+			h = vload(&I.heads[v]);
+			live = (h >> kTagShift) == tag && (long long)(h & kIdxMask) < end;
 		}
+		const unsigned ball = __ballot_sync(0xffffffffu, live);
+		if (ball == 0)
+			return nf;
+		const int src = __ffs(ball) - 1;
+		long long got = -1;
+		if (lane == src && atomicCAS(&I.heads[v], h, h + 1) == h)
+			got = (long long)(h & kIdxMask);
+		got = __shfl_sync(0xffffffffu, got, src);
+		if (got >= 0)
+			return got;
 	}
-	return nf;
 }
 
 // Bounds fathers of instance I's open phase `ph` in this CTA (tables of I
@@ -213,10 +234,13 @@ __device__ void bound_phase(const ResInst &I, unsigned long long ph, int own, ui
 {
 	constexpr int NT = staged::kFamThreads;
 	__shared__ long long s_first[kResGroups];
-	const long long nf = (long long)(ph & kIdxMask);
+	const long long nf = (long long)(ph & kNfMask);
 	const int group = int(threadIdx.x) / NT;
-	if (threadIdx.x % NT == 0)
-		s_first[group] = group < I.L.groups ? claim_father(I, ph, own) : nf;
+	if (threadIdx.x % NT < 32) { // the group's first warp
+		const long long c = group < I.L.groups ? claim_father(I, ph, own) : nf;
+		if (threadIdx.x % NT == 0)
+			s_first[group] = c;
+	}
 	__syncthreads();
 	const long long first = s_first[group];
 	long long done = 0;
@@ -284,17 +308,21 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 			return;
 		make_children_body(I.P, 0, (long long)rank * kResThreads + tid,
 		                   (long long)nc * kResThreads);
-		// open the family phase: pools of this iteration's fathers, one per
-		// CTA of the group, under a new tag
+		// open the family phase: pools of this iteration's fathers under a
+		// new tag
 		if (!group_barrier(I, G, [&] {
 			    const long long nf = vload(&D->n_fathers);
+			    const int np = int(max(1ll, min((long long)kMaxPools, nf / kFathersPerPool)));
 			    // tags 1 .. 2^24 - 1 (a closed pool counter reads tag 0)
 			    const unsigned long long tag = (unsigned long long)(it % 0xffffff) + 1;
 			    S->fam_done = 0;
-			    for (int v = 0; v < nc; ++v)
-				    atomicExch(&I.heads[v], tag << kTagShift | (unsigned long long)pool_start(nf, v, nc));
+			    for (int v = 0; v < np; ++v)
+				    atomicExch(&I.heads[v], tag << kTagShift | (unsigned long long)pool_start(nf, v, np));
 			    __threadfence();
-			    atomicExch(&S->phase, nf > 0 ? (tag << kTagShift | (unsigned long long)nf) : 0ull);
+			    atomicExch(&S->phase, nf > 0 ? (tag << kTagShift |
+			                                    (unsigned long long)np << kPoolShift |
+			                                    (unsigned long long)nf)
+			                                 : 0ull);
 			    return 1;
 		    }))
 			return;
@@ -306,11 +334,12 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 		// close it once every father is bounded, thieves' included
 		if (!group_barrier(I, G, [&] {
 			    const unsigned long long ph = vload(&S->phase);
-			    const unsigned long long nf = ph & kIdxMask;
+			    const unsigned long long nf = ph & kNfMask;
+			    const int np = int((ph & kIdxMask) >> kPoolShift);
 			    const int ok = ph == 0 ||
 			                   bounded_wait(I, G, [&] { return vload(&S->fam_done) >= nf; });
 			    atomicExch(&S->phase, 0ull);
-			    for (int v = 0; v < nc; ++v)
+			    for (int v = 0; v < np; ++v)
 				    atomicExch(&I.heads[v], 0ull);
 			    __threadfence();
 			    return ok;
@@ -340,14 +369,17 @@ __global__ void __launch_bounds__(kResThreads)
                     ResGlobal *G)
 {
 	extern __shared__ __align__(16) uint8_t smem[];
-	const int g = cta_inst[blockIdx.x];
-	const ResInst &I = insts[g];
-	run_instance(I, int(blockIdx.x) - I.first_cta, G, smem);
-	__syncthreads();
-	if (threadIdx.x == 0 && int(blockIdx.x) == I.first_cta) {
-		__threadfence();
-		atomicAdd(&G->finished, 1u);
+	const int g = cta_inst[blockIdx.x]; // -1: a CTA outside every group
+	if (g >= 0) {
+		const ResInst &I = insts[g];
+		run_instance(I, int(blockIdx.x) - I.first_cta, G, smem);
+		__syncthreads();
+		if (threadIdx.x == 0 && int(blockIdx.x) == I.first_cta) {
+			__threadfence();
+			atomicAdd(&G->finished, 1u);
+		}
 	}
+	const int g0 = g >= 0 ? g : int(blockIdx.x) % K; // where its search for fathers starts
 	// then help the instances still running, until every one has ended
 	__shared__ int s_go;
 	__shared__ unsigned long long s_ph;
@@ -362,7 +394,7 @@ __global__ void __launch_bounds__(kResThreads)
 				s_go = 1;
 				s_j = -1;
 				for (int k = 1; k <= K; ++k) {
-					const int j = (g + k + round) % K;
+					const int j = (g0 + k + round) % K;
 					const unsigned long long ph = vload(&insts[j].sync->phase);
 					if (ph) {
 						s_j = j;
@@ -384,7 +416,7 @@ __global__ void __launch_bounds__(kResThreads)
 		const int j = s_j;
 		if (j < 0) {
 			if (threadIdx.x == 0)
-				__nanosleep(1000);
+				__nanosleep(200);
 			continue;
 		}
 		if (threadIdx.x == 0)
@@ -396,7 +428,7 @@ __global__ void __launch_bounds__(kResThreads)
 			staged::staged_load_tables(J.bp, J.tpack, J.L, smem);
 			staged_for = j;
 		}
-		bound_phase(J, s_ph, (int(blockIdx.x) * 7) % J.num_ctas, smem);
+		bound_phase(J, s_ph, int(blockIdx.x), smem);
 		__syncthreads();
 	}
 }
@@ -517,17 +549,21 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 		return wsbb_set_error(c0, WSBB_ERR_ARG,
 		                      "resident search: more instances than resident CTAs (" +
 		                          std::to_string(grid) + ")");
-	// groups: an equal share of the CTAs per instance
-	std::vector<int16_t> cta_inst((size_t)grid);
-	int at = 0, heads = 0;
+	// groups: an equal share of the CTAs per instance, at most group_ctas
+	// when the caller sets it; the CTAs left over take fathers from every
+	// instance's bound phase (for one instance the whole grid in its group
+	// is the fastest: its bound phase gains more than its barriers lose)
+	const int group_cap = opts && opts->group_ctas > 0 ? opts->group_ctas : grid;
+	std::vector<int16_t> cta_inst((size_t)grid, int16_t(-1));
+	int at = 0;
+	const int heads = kMaxPools * count;
 	for (int k = 0; k < count; ++k) {
-		const int nc = grid / count + (k < grid % count ? 1 : 0);
+		const int nc = std::min(grid / count + (k < grid % count ? 1 : 0), group_cap);
 		H[size_t(k)].first_cta = at;
 		H[size_t(k)].num_ctas = nc;
 		for (int b = 0; b < nc; ++b)
 			cta_inst[size_t(at + b)] = int16_t(k);
 		at += nc;
-		heads += nc;
 	}
 	// device copies: instances, their sync words and pool counters, the
 	// CTA map, the launch's own words
@@ -543,10 +579,9 @@ extern "C" int wsbb_explore_resident(wsbb_ctx *const *ctxs, int count,
 		return wsbb_set_error(c0, WSBB_ERR_NOMEM, "resident search buffers");
 	ResSync *d_sync = reinterpret_cast<ResSync *>(mem + off_sync);
 	unsigned long long *d_heads = reinterpret_cast<unsigned long long *>(mem + off_heads);
-	for (int k = 0, h = 0; k < count; ++k) {
+	for (int k = 0; k < count; ++k) {
 		H[size_t(k)].sync = d_sync + k;
-		H[size_t(k)].heads = d_heads + h;
-		h += H[size_t(k)].num_ctas;
+		H[size_t(k)].heads = d_heads + size_t(k) * kMaxPools;
 	}
 	ResGlobal glob{};
 	glob.self_test = self_test;

@@ -45,7 +45,7 @@ RESIDENT = 8   # run as the resident search (one cooperative launch)
 
 
 class ResidentOpts(C.Structure):
-    _fields_ = [("wait_ms", C.c_int32), ("self_test", C.c_int32)]
+    _fields_ = [("wait_ms", C.c_int32), ("self_test", C.c_int32), ("group_ctas", C.c_int32)]
 
 
 def coverage(hist, n: int) -> int:
@@ -85,10 +85,12 @@ def explore(ctx: Context, ub0: int | None = None, best: int = 99999, window: int
 
 def explore_resident(ctxs, ub0s=None, bests=None, window: int = 0, capacity: int = 0,
                      max_iters: int = 0, max_bounded=0, wait_ms: int = 0,
-                     self_test: bool = False, stream: int = 0, check: bool = True):
+                     self_test: bool = False, stream: int = 0, check: bool = True,
+                     group_ctas: int = 0):
     """Search every context's instance in one launch of resident CTAs
-    (wsbb_explore_resident): a group of CTAs per instance, fathers stolen
-    between CTAs and from instances still running. `ub0s`, `bests`,
+    (wsbb_explore_resident): a group of at most `group_ctas` CTAs per
+    instance (0: the library's default), fathers stolen between CTAs and
+    from instances still running. `ub0s`, `bests`,
     `capacity`, `max_iters` and `max_bounded` may be one value for all or
     one per context. Returns
     (return code, [stats dict per instance]); with `check`, a failure
@@ -108,7 +110,7 @@ def explore_resident(ctxs, ub0s=None, bests=None, window: int = 0, capacity: int
                               for i in range(k)])
     hs = (C.c_void_p * k)(*[c.h for c in ctxs])
     st = (ExploreStats * k)()
-    opts = ResidentOpts(int(wait_ms), 1 if self_test else 0)
+    opts = ResidentOpts(int(wait_ms), 1 if self_test else 0, int(group_ctas))
     rc = L.wsbb_explore_resident(hs, k, cfgs, C.byref(opts), st, stream or None)
     if rc != 0 and check:
         raise WsbbError(rc, L.wsbb_last_error(ctxs[0].h).decode())
