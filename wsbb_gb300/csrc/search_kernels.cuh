@@ -584,43 +584,56 @@ __device__ void doom_body(const ExParams &P)
 	const long long stop = max(-1ll, top - P.region_cap);
 	int dd = -1;              // depth of the open condemned subtree's marker (-1: none)
 	long long dd_at = -1;     // its stack index
-	for (long long base = top; base > stop; base -= 32) {
-		const long long idx = base - lane;
-		const bool valid = idx > stop;
-		Meta e = {0, 0, ST_DEAD, 0};
-		if (valid)
-			e = P.meta[idx];
-		const int depth = e.depth;
-		const unsigned condemned =
-		    __ballot_sync(0xffffffffu, valid && e.state == ST_BRANCHED && e.lb >= ub);
-		unsigned dead = 0;
-		int from = 0; // lanes before `from` are settled for this step
-		for (;;) {
-			const unsigned rest = from >= 32 ? 0u : (0xffffffffu << from);
-			if (dd >= 0) {
-				const unsigned closer = __ballot_sync(0xffffffffu, valid && depth <= dd) & rest;
-				if (!closer) {
-					dead |= __ballot_sync(0xffffffffu, valid) & rest;
-					break; // the subtree goes on past this step
-				}
-				const int c = __ffs(closer) - 1;
-				dead |= rest & ~(0xffffffffu << c); // lanes [from, c)
-				if (lane == 0)
-					P.meta[dd_at].state = ST_CONDEMNED;
-				dd = -1;
-				from = c; // the closing entry may open a subtree itself
-				continue;
-			}
-			const unsigned opener = condemned & rest;
-			if (!opener)
-				break;
-			const int o = __ffs(opener) - 1;
-			dd = __shfl_sync(0xffffffffu, depth, o);
-			dd_at = base - o;
-			from = o + 1;
+	// kDoomSteps steps of 32 entries are loaded at once (a step writes only
+	// entries at or above its own, never the ones loaded for later steps)
+	constexpr int kDoomSteps = 8;
+	for (long long base0 = top; base0 > stop; base0 -= 32 * kDoomSteps) {
+		Meta eb[kDoomSteps];
+#pragma unroll
+		for (int b = 0; b < kDoomSteps; ++b) {
+			const long long idx = base0 - 32 * b - lane;
+			eb[b] = idx > stop ? P.meta[idx] : Meta{0, 0, ST_DEAD, 0};
 		}
-		if (valid && ((dead >> lane) & 1u))
-			P.meta[idx].state = ST_DEAD;
+#pragma unroll
+		for (int b = 0; b < kDoomSteps; ++b) {
+			const long long base = base0 - 32 * b;
+			if (base <= stop)
+				break; // uniform
+			const long long idx = base - lane;
+			const bool valid = idx > stop;
+			const Meta e = eb[b];
+			const int depth = e.depth;
+			const unsigned condemned =
+			    __ballot_sync(0xffffffffu, valid && e.state == ST_BRANCHED && e.lb >= ub);
+			unsigned dead = 0;
+			int from = 0; // lanes before `from` are settled for this step
+			for (;;) {
+				const unsigned rest = from >= 32 ? 0u : (0xffffffffu << from);
+				if (dd >= 0) {
+					const unsigned closer = __ballot_sync(0xffffffffu, valid && depth <= dd) & rest;
+					if (!closer) {
+						dead |= __ballot_sync(0xffffffffu, valid) & rest;
+						break; // the subtree goes on past this step
+					}
+					const int c = __ffs(closer) - 1;
+					dead |= rest & ~(0xffffffffu << c); // lanes [from, c)
+					if (lane == 0)
+						P.meta[dd_at].state = ST_CONDEMNED;
+					dd = -1;
+					from = c; // the closing entry may open a subtree itself
+					continue;
+				}
+				const unsigned opener = condemned & rest;
+				if (!opener)
+					break;
+				const int o = __ffs(opener) - 1;
+				dd = __shfl_sync(0xffffffffu, depth, o);
+				dd_at = base - o;
+				from = o + 1;
+			}
+			if (valid && ((dead >> lane) & 1u))
+				P.meta[idx].state = ST_DEAD;
+		}
 	}
 	// a subtree that runs to the stack bottom also ended inside the walk
 	if (dd >= 0 && stop < 0 && lane == 0)
