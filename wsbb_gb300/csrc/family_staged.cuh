@@ -1,6 +1,6 @@
 // Family bounds, staged form (see family.cu for the method): the device
 // code shared by the standalone kernel (family.cu, wsbb_decompose_lb2 and the
-// graph-launched search) and the resident search (explore.cu), which bounds
+// graph-launched search) and the resident search (resident.cu), which bounds
 // the fathers of many instances from CTAs that stay resident.
 #pragma once
 
@@ -23,13 +23,14 @@ constexpr int kWalkThreads = kFamThreads - kFrontThreads;
 constexpr int kMaxCtaThreads = 768;
 constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 
-//// The same bounds, organised around shared memory (plain bounds of fathers
+// The same bounds, organised around shared memory (plain bounds of fathers
 // whose pairs fit the walkers, P <= 192, with times that pack into the
 // 32-bit Johnson entries of DeviceTables::tpack and 16-bit staircase paths):
 //
-//  * the packed Johnson table is staged once per CTA, position-major with
-//    rows of Pp (a multiple of 64) words, so a warp of walkers (consecutive
-//    pairs) reading entries at any positions hits 32 distinct banks;
+//  * the packed Johnson table is staged once per CTA (for all its
+//    groups), position-major with rows of Pp (a multiple of 64) words, so a
+//    warp of walkers (consecutive pairs) reading entries at any positions
+//    hits 32 distinct banks;
 //  * the forward pass leaves, per walk rank k, the prefix C (16 bits) and
 //    the position q in rows [k][Pp] (lanes walk in step, so these accesses
 //    are conflict-free too) and the backward pass reads them back instead

@@ -38,13 +38,14 @@ namespace {
 // instance, so one launch searches many instances. A group's CTAs meet at
 // group barriers between the phases; the phases that take one CTA (commit
 // and doom, plan, kept scan, finish) run on the group's first CTA. In the
-// family phase each CTA of the group owns a pool of the iteration's fathers
-// (a contiguous share) and, once its own pool is empty, steals from its
-// group's other pools; CTAs whose instance has finished steal fathers from
-// the family phases of the instances still running, so a launch keeps every
-// SM busy until the last instance ends. Every wait between CTAs is bounded
-// by a %globaltimer limit; one that runs out sets WSBB_ERR_WATCHDOG on its
-// instance and aborts the launch, every CTA leaving at its next wait.
+// family phase the iteration's fathers are split into pools; each CTA
+// starts at a pool of its own and moves on to the others when it is empty;
+// CTAs outside every group, and those whose instance has finished, steal
+// fathers from the family phases of the instances still running, so a
+// launch keeps every SM busy until the last instance ends. Every wait
+// between CTAs is bounded by a %globaltimer limit; one that runs out
+// records WSBB_ERR_WATCHDOG for its instance and aborts the launch, every
+// CTA leaving at its next wait.
 
 // Father pools: a phase's fathers are split into pools of about
 // kFathersPerPool (at most kMaxPools, one per lane of a warp), each with a
