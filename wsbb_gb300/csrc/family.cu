@@ -708,11 +708,11 @@ __global__ void __launch_bounds__(staged::kMaxCtaThreads, 1)
 	const long long groups = L.groups;
 	if ((long long)blockIdx.x >= nf)
 		return;
-	staged::staged_load_tables(bp, tpack, L, smem);
+	staged::staged_load_tables(bp, tpack, jobposT, L, smem);
 	__syncthreads();
 	const int group = int(threadIdx.x) / NT;
 	const long long base = (long long)gridDim.x * groups;
-	staged::staged_fathers<kWide, NT>(A, bp, jobposT, L, smem, group, nf,
+	staged::staged_fathers<kWide, NT>(A, bp, L, smem, group, nf,
 	                                  (long long)group * gridDim.x + blockIdx.x,
 	                                  [&](long long after) -> long long {
 		                                  // one warp calls it: lane 0 claims for all

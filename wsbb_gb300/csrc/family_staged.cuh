@@ -43,12 +43,12 @@ constexpr int32_t kNeg = -(1 << 28); // max-plus -inf, far from any sum of times
 //    and both children's three terms are computed as 16-bit halves of one
 //    word (add, then one three-way and one two-way unsigned 16-bit
 //    maximum).
-// The CTA's tables first (T, heads and tails, processing times, pairs),
-// then one region per group, `grp_bytes` apart from `off_grp`; the offsets
-// Xr ... misc lie within a group's region.
+// The CTA's tables first (T, heads and tails, processing times, pairs, the
+// job positions per pair), then one region per group, `grp_bytes` apart from
+// `off_grp`; the offsets Xr ... misc lie within a group's region.
 struct StagedLayout {
 	int Pp, xcs, xvs, frs, groups;
-	size_t off_T, off_HT, off_pt, off_pairs, off_grp, grp_bytes;
+	size_t off_T, off_HT, off_pt, off_pairs, off_JP, off_grp, grp_bytes;
 	size_t off_Xr, off_Xq, off_Xc, off_VW, off_PK, off_F, off_G, off_fr, off_misc;
 	size_t bytes;
 };
@@ -70,6 +70,8 @@ inline StagedLayout staged_layout(int n, int m, int P, int Pp, int groups = 1)
 	off = a16(off + size_t(m) * (n + 1) * 2);
 	L.off_pairs = off;
 	off = a16(off + size_t(P) * 4);
+	L.off_JP = off; // jobposT: the position of job j in pair p's order at [j][P]
+	off = a16(off + size_t(n) * P);
 	L.off_grp = off;
 	off = 0; // a group's region
 	L.off_Xr = off; // the cross-slice reduction reuses it after the backward pass
@@ -232,11 +234,12 @@ constexpr int kSB = 4; // staged walks and sweep: entries loaded ahead per batch
 
 
 // Stages one instance's tables for staged_fathers: the packed Johnson
-// table, processing times, pairs, heads and tails. Every thread of the CTA
-// calls it; a barrier of the whole CTA must follow before staged_fathers
-// reads them.
+// table, processing times, pairs, heads and tails, job positions. Every
+// thread of the CTA calls it; a barrier of the whole CTA must follow before
+// staged_fathers reads them.
 __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
                                                    const uint32_t *__restrict__ tpack,
+                                                   const uint8_t *__restrict__ jobposT,
                                                    const StagedLayout &L, uint8_t *smem)
 {
 	const int n = bp.n, m = bp.m, P = bp.P, tid = threadIdx.x;
@@ -257,6 +260,8 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 		sPt[(i / n) * (n + 1) + i % n] = uint16_t(g_pt[i]);
 	for (int i = tid; i < P; i += int(blockDim.x))
 		sPairs[i] = g_pairs[i];
+	for (int i = tid; i < n * P; i += int(blockDim.x))
+		smem[L.off_JP + i] = __ldg(jobposT + i);
 	if (tid < m) {
 		sHT[tid] = g_heads[tid];
 		sHT[32 + tid] = g_tails[tid];
@@ -284,7 +289,7 @@ __device__ __forceinline__ void staged_load_tables(const BoundParams &bp,
 // sub-partitions (warp slot mod 4) and the walkers spread evenly over them.
 template <bool kWide, int NT, typename Claim>
 __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
-                                    const uint8_t *__restrict__ jobposT, const StagedLayout &L,
+                                    const StagedLayout &L,
                                     uint8_t *smem, int group, long long nf, long long first,
                                     Claim claim)
 {
@@ -311,6 +316,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 	int16_t *sFrBuf = reinterpret_cast<int16_t *>(gsm + L.off_fr); // [2][L.frs]
 	uint32_t *sMaskBuf = reinterpret_cast<uint32_t *>(gsm + L.off_misc); // [2][4]
 	long long *sNext = reinterpret_cast<long long *>(gsm + L.off_misc + 32); // [2]
+	const uint8_t *sJP = smem + L.off_JP;
 	auto sync = [group]() { group_sync<NT>(group); };
 
 	// record of father g into buffer b, and its free jobs into job mask b
@@ -452,13 +458,13 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 					uint64_t m64 = 0;
 #pragma unroll 4
 					for (int i = 0; i < u; ++i)
-						m64 |= 1ull << __ldg(jobposT + (size_t)fj[i] * P + t);
+						m64 |= 1ull << sJP[fj[i] * P + t];
 					w[0] = uint32_t(m64);
 					w[NW - 1] = uint32_t(m64 >> 32);
 				} else {
 #pragma unroll 4
 					for (int i = 0; i < u; ++i) {
-						const int q = __ldg(jobposT + (size_t)fj[i] * P + t);
+						const int q = sJP[fj[i] * P + t];
 #pragma unroll
 						for (int wi = 0; wi < NW; ++wi)
 							w[wi] |= (q >> 5) == wi ? 1u << (q & 31) : 0u;

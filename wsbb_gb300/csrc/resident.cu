@@ -247,9 +247,9 @@ __device__ void bound_phase(const ResInst &I, unsigned long long ph, int own, ui
 	long long done = 0;
 	if (first < nf) { // uniform in the group
 		auto claim = [&](long long) { return claim_father(I, ph, own); };
-		done = I.wide ? staged::staged_fathers<true, NT>(I.FA, I.bp, I.jobposT, I.L, smem, group,
+		done = I.wide ? staged::staged_fathers<true, NT>(I.FA, I.bp, I.L, smem, group,
 		                                                 nf, first, claim)
-		              : staged::staged_fathers<false, NT>(I.FA, I.bp, I.jobposT, I.L, smem, group,
+		              : staged::staged_fathers<false, NT>(I.FA, I.bp, I.L, smem, group,
 		                                                  nf, first, claim);
 	}
 	__threadfence(); // the group's child bounds, before they are counted
@@ -268,7 +268,7 @@ __device__ void run_instance(const ResInst &I, int rank, ResGlobal *G, uint8_t *
 	const int nc = I.num_ctas, tid = threadIdx.x;
 	const bool body = tid < kResBodyThreads; // the threads that run the bodies
 	ResSync *S = I.sync;
-	staged::staged_load_tables(I.bp, I.tpack, I.L, smem);
+	staged::staged_load_tables(I.bp, I.tpack, I.jobposT, I.L, smem);
 	// the watchdog self-test: the first barrier also waits for a flag that
 	// nothing sets
 	if (!group_barrier(I, G, [&] {
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(kResThreads)
 		const ResInst &J = insts[j];
 		if (staged_for != j) {
 			__syncthreads();
-			staged::staged_load_tables(J.bp, J.tpack, J.L, smem);
+			staged::staged_load_tables(J.bp, J.tpack, J.jobposT, J.L, smem);
 			staged_for = j;
 		}
 		bound_phase(J, s_ph, int(blockIdx.x), smem);
