@@ -91,8 +91,9 @@ inline StagedLayout staged_layout(int n, int m, int P, int Pp, int groups = 1)
 	L.frs = (n + 4 + 7) & ~7; // two record buffers
 	L.off_fr = off;
 	off = a16(off + size_t(2 * L.frs) * 2);
-	L.off_misc = off; // two 4-word job masks, then two claimed fathers
-	off += 32 + 16;
+	// two 4-word job masks, two claimed fathers, two child ranges
+	L.off_misc = off;
+	off += 32 + 16 + 32;
 	L.grp_bytes = a16(off);
 	L.bytes = L.off_grp + size_t(groups) * L.grp_bytes;
 	return L;
@@ -316,16 +317,19 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 	int16_t *sFrBuf = reinterpret_cast<int16_t *>(gsm + L.off_fr); // [2][L.frs]
 	uint32_t *sMaskBuf = reinterpret_cast<uint32_t *>(gsm + L.off_misc); // [2][4]
 	long long *sNext = reinterpret_cast<long long *>(gsm + L.off_misc + 32); // [2]
+	long long *sKids = reinterpret_cast<long long *>(gsm + L.off_misc + 48); // [2][2]
 	const uint8_t *sJP = smem + L.off_JP;
 	auto sync = [group]() { group_sync<NT>(group); };
 
-	// record of father g into buffer b, and its free jobs into job mask b
-	// (zeroed before); job ids clamped to [0, n): a malformed record gives
-	// wrong bounds, never an access outside the tables. Threads t0 .. t0 +
-	// nt - 1.
+	// record of father g into buffer b, its free jobs into job mask b
+	// (zeroed before) and its child range into sKids[b]; job ids clamped to
+	// [0, n): a malformed record gives wrong bounds, never an access outside
+	// the tables. Threads t0 .. t0 + nt - 1.
 	auto load_record = [&](long long g, int b, int t0, int nt) {
 		if (g >= nf)
 			return;
+		if (tid - t0 < 2)
+			sKids[2 * b + tid - t0] = A.child_off[g + tid - t0];
 		const long long ri = A.ridx ? A.ridx[g] : g;
 		const int16_t *g_fr = reinterpret_cast<const int16_t *>(A.fathers + ri * A.stride);
 		int16_t *dst = sFrBuf + b * L.frs;
@@ -357,7 +361,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		uint32_t *sMask = sMaskBuf + 4 * cur;
 		const int l1 = sFr[n], l2 = sFr[n + 1];
 		const int u = l2 - l1 - 1;
-		const long long c0 = A.child_off[f];
+		const long long c0 = sKids[2 * cur];
 		// the other mask buffer (its father is done) is cleared for the
 		// next record, which prefetch() loads after a barrier at least
 		if (tid < 4)
@@ -376,7 +380,7 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 		};
 		// cursors outside -1 <= l1, l2 <= n with two free jobs or more, or a
 		// child range of another size: the father is skipped
-		if (l1 < -1 || l2 > n || u < 2 || A.child_off[f + 1] - c0 != (u == 2 ? 2 : 2 * u)) {
+		if (l1 < -1 || l2 > n || u < 2 || sKids[2 * cur + 1] - c0 != (u == 2 ? 2 : 2 * u)) {
 			sync(); // the other mask is clear
 			prefetch();
 			++done;
