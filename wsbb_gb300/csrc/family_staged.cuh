@@ -160,7 +160,7 @@ __device__ __forceinline__ bool mask_has(const uint32_t (&w)[NW], int job)
 // max(its own time, lane k-1's); the times of kWaveBatch steps are loaded
 // before their steps run, so that only the steps' own chain (a shuffle, a
 // maximum and an add) is serial.
-constexpr int kWaveBatch = 8;
+constexpr int kWaveBatch = 4;
 template <typename TimeOf>
 __device__ __forceinline__ int32_t staged_wave(int lane, int m, int nj, TimeOf time_of)
 {
@@ -231,7 +231,11 @@ __device__ __forceinline__ void staged_fronts(int warp, int lane, int n, int m, 
 	}
 }
 
-constexpr int kSB = 4; // staged walks and sweep: entries loaded ahead per batch
+// Staged walks and sweep: entries loaded ahead per batch. One: with three
+// groups per SM the other warps hide a load's latency, and batches of 2 or
+// 4 only added registers and predicated slots past the last entry (the
+// search 11 % slower with 4, 5 % with 2).
+constexpr int kSB = 1;
 
 
 // Stages one instance's tables for staged_fathers: the packed Johnson
@@ -474,8 +478,8 @@ __device__ long long staged_fathers(const FamilyArgs &A, const BoundParams &bp,
 							w[wi] |= (q >> 5) == wi ? 1u << (q & 31) : 0u;
 					}
 				}
-				// batches of kSB: positions first, then their entries (the
-				// loads in flight together), then the recurrence
+				// batches of kSB: positions first, then their entries, then
+				// the recurrence
 				for (int k0 = 0; k0 < u; k0 += kSB) {
 					int q[kSB];
 					uint32_t e[kSB];
